@@ -1,0 +1,363 @@
+"""Benchmark of the lattice max-flow engine on one GB300 (or N replicas).
+
+Default workload: the single large 2-d cut, 2048x2048 Full2d_8, int32
+capacities (seeded synthetic image, see latticeflow_gb300/workloads.py).
+A step is one complete exact solve: clear the lattice, fill the energies,
+push-relabel to a maximum preflow, both canonical cut sets, flow value.
+
+  value  solves/s with the energies already resident in HBM
+  e2e    the same through the reference-facing C-ABI call with host buffers:
+         addEnergyPotentials from pinned host int64 arrays (H2D inside the
+         step) and the cut read back to the host (D2H inside the step)
+
+Multi-GPU: independent replicas (the path has no exchange step); value is the
+solves of all ranks over the max-over-ranks time ("scaling": "weak").
+
+--impl reference times the reference algorithm on the host cores instead:
+the CPU restatement of the reference push-relabel (oracle port), one solve per
+host core in parallel per step.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "max-flow solves/s & HBM GB/s, batched vs plain on GB300 (exact cut); TV p99 ms"
+UNIT = "solves/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="large_cut",
+                    choices=["large_cut", "plain_cut", "volume_cut"])
+    ap.add_argument("--seed", type=int, default=0)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_workload(name, seed):
+    from latticeflow_gb300 import workloads as W
+    if name == "large_cut":
+        return W.large_cut(seed)
+    if name == "plain_cut":
+        return W.plain_cut(seed)
+    if name == "volume_cut":
+        return W.volume_cut(seed)
+    raise ValueError(name)
+
+
+def workload_config(name, p):
+    return {"workload": name, "kernel": p.kernel, "shape": list(p.dims), "capacity": "int32",
+            "seed": 0, "l2": "inputs larger than L2 (no flush needed)"}
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler(object):
+    """nvidia-smi samples during the timed region (read only)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(kernel_key):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        v = d.get(kernel_key)
+        if isinstance(v, dict):
+            return v
+    return None
+
+
+# ---------------------------------------------------------------- ours
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from latticeflow_gb300 import _build
+    _build.build_native()
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import _native as N
+
+    p = make_workload(args.workload, args.seed)
+    u, b = p.energies()
+    hu = torch.from_numpy(u).pin_memory()
+    hb = torch.from_numpy(b).pin_memory()
+    du = hu.cuda()
+    db = hb.cuda()
+    torch.cuda.synchronize()
+    L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    lib = N.lib()
+    h = L._h
+    stream = torch.cuda.ExternalStream(L.stream())
+
+    def step_device():
+        N.check(lib.lf_clear(h))
+        N.check(lib.lf_add_energy_potentials_device(h, ctypes.c_void_p(du.data_ptr()),
+                                                    ctypes.c_void_p(db.data_ptr())))
+        N.check(lib.lf_run(h))
+        return L.flow()
+
+    cut = np.empty(p.n, dtype=np.int32)
+
+    def step_e2e():
+        N.check(lib.lf_clear(h))
+        N.check(lib.lf_add_energy_potentials(h, ctypes.c_void_p(hu.data_ptr()),
+                                             ctypes.c_void_p(hb.data_ptr())))
+        N.check(lib.lf_run(h))
+        N.check(lib.lf_get_cut(h, cut.ctypes.data_as(ctypes.c_void_p)))
+        return L.flow()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed(fn, steps, profile):
+        barrier()
+        torch.cuda.synchronize()
+        L.setProfiling(profile)
+        prof = {"pr_ms": 0.0, "bfs_ms": 0.0, "reach_ms": 0.0, "pr_tiles": 0, "pr_launches": 0,
+                "bfs_passes": 0, "bfs_tiles": 0}
+        k0 = L.profile()["kernel_launches"]
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        res = None
+        for _ in range(steps):
+            res = fn()
+            pr = L.profile()
+            for k in prof:
+                prof[k] += pr[k]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        launches = L.profile()["kernel_launches"] - k0
+        L.setProfiling(False)
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        barrier()
+        return ms, res, prof, launches
+
+    for _ in range(args.warmup):
+        step_device()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms, res, prof, launches = timed(step_device, args.steps, True)
+    clocks = sampler.stop()
+    for _ in range(max(1, args.warmup)):
+        step_e2e()
+    ms_e2e, _, _, _ = timed(step_e2e, args.steps, False)
+
+    tile, padded, elem = L.layout()
+    nt = tile[0] * tile[1] * tile[2]
+    K = 2 * L.nFillingEdges
+    peak, peak_kind = measured_peaks()
+    pr_bytes = prof["pr_tiles"] * nt * 2 * (K * elem + elem + 4)
+    bfs_bytes = prof["bfs_tiles"] * nt * (8 + 4 + 4)
+    if prof["pr_ms"] >= prof["bfs_ms"]:
+        kname, kbytes, kms, klaunch = "k_pr_tile", pr_bytes, prof["pr_ms"], prof["pr_launches"]
+    else:
+        kname, kbytes, kms, klaunch = "k_bfs_tile", bfs_bytes, prof["bfs_ms"], prof["bfs_passes"]
+    achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else 0.0
+    tr = committed_traffic(args.workload + ":" + kname)
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs, copy)",
+                "traffic": tr.get("dram_bytes_per_launch") if tr else None,
+                "algorithmic_bytes_per_launch": int(kbytes / max(1, klaunch)),
+                "kernel_ms_share": round(kms / max(ms, 1e-9), 3),
+                "launches": int(klaunch)}
+
+    value = world * args.steps / (ms * 1e-3)
+    e2e_value = world * args.steps / (ms_e2e * 1e-3)
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator, latticeflow_gb300/workloads.py)",
+        "config": dict(workload_config(args.workload, p), parallelism="replicas" if world > 1 else "single"),
+        "e2e": {"value": round(e2e_value, 4), "unit": UNIT,
+                "h2d_bytes_per_step": int(u.nbytes + b.nbytes),
+                "d2h_bytes_per_step": int(2 * p.n * 4 + 64)},
+        "roofline": roofline,
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+        "solver": {"flow": res[0], "energy": res[1], "profile_ms": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in prof.items()},
+                   "tile": list(tile), "elem_bytes": elem},
+    }
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline(p)
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_baseline(p, budget_s=12.0):
+    """Restated reference push-relabel on one host core, same workload."""
+    from oracle import oracle as O
+    O.build_port()
+    u, b = p.energies()
+    times = []
+    t0 = time.time()
+    while not times or (time.time() - t0 < budget_s and len(times) < 20):
+        _, secs = O.port_pr(p.kernel, p.dims, u, b)
+        times.append(secs)
+    return {"value": round(len(times) / sum(times), 4), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d full solves of the same workload, reference push-relabel restated "
+                      "(oracle/lf_oracle.cpp), median %.3f s" % (len(times), float(np.median(times)))}
+
+
+# ---------------------------------------------------------------- reference
+
+_W = {}
+
+
+def _ref_init(workload, seed):
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    O.port()
+    p = make_workload(workload, seed)
+    _W["p"] = p
+    _W["e"] = p.energies()
+
+
+def _ref_solve(_):
+    from oracle import oracle as O
+    p = _W["p"]
+    u, b = _W["e"]
+    _, secs = O.port_pr(p.kernel, p.dims, u, b)
+    return secs
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle import oracle as O
+    O.build_port()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    p = make_workload(args.workload, args.seed)
+    with ctx.Pool(cores, initializer=_ref_init, initargs=(args.workload, args.seed)) as pool:
+        for _ in range(args.warmup):
+            pool.map(_ref_solve, range(cores), chunksize=1)
+        t0 = time.time()
+        for _ in range(args.steps):
+            pool.map(_ref_solve, range(cores), chunksize=1)
+        wall = time.time() - t0
+    value = cores * args.steps / wall
+    kind = "port"
+    out = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * wall / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+        "data": "synthetic (seeded generator, latticeflow_gb300/workloads.py)",
+        "config": workload_config(args.workload, p),
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": "each step: one full solve per host core in parallel "
+                                   "(reference push-relabel restated, oracle/lf_oracle.cpp)"},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

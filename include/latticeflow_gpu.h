@@ -1,0 +1,163 @@
+/*
+ * latticeflow_gpu.h -- C ABI of the GB300 lattice max-flow engine.
+ *
+ * Plain pointers and sizes only; every entry point returns an LF_* status
+ * code (0 = LF_OK) unless noted, and lf_last_error() gives the message of the
+ * last failure on the calling thread.  One handle owns one CUDA stream and
+ * all of its device state; a handle is not thread-safe, different handles are
+ * independent.  All array arguments are HOST pointers unless the name ends in
+ * _device.
+ *
+ * Each entry point names the reference interface it replaces (paths within
+ * the latticeflow project).
+ */
+#ifndef LATTICEFLOW_GPU_H
+#define LATTICEFLOW_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The C++ adapter turns LF_ERR_BAD_NAME into
+ * BadSolverOrKernelName (solver/interface.hpp:152-168) and LF_ERR_RANGE from
+ * the TV path into std::out_of_range (solver/tv/tv_solver.hpp:202-206). */
+enum {
+  LF_OK = 0,
+  LF_ERR_BAD_NAME = 1,       /* unknown solver or kernel name               */
+  LF_ERR_SHAPE = 2,          /* dimension count / sizes do not fit          */
+  LF_ERR_RANGE = 3,          /* value outside the representable range,
+                                non-submodular pairwise term, bad lambda     */
+  LF_ERR_NO_CONVERGENCE = 4, /* an iteration cap was reached                */
+  LF_ERR_OOM = 5,            /* device allocation failed                    */
+  LF_ERR_CUDA = 6,           /* other CUDA runtime error                    */
+  LF_ERR_INVALID = 7,        /* null handle / pointer, bad argument         */
+  LF_ERR_STATE = 8           /* call out of order (e.g. getCut before run)  */
+};
+
+typedef struct lf_lattice lf_lattice;
+
+/* Last error message on this thread ("" if none). */
+const char* lf_last_error(void);
+
+/* ------------------------------------------------------------------ factory
+ * solver/interface.hpp:170-191 and the generated factory
+ * (install/templates/factory/file.cpp:26-95).  Solver names accepted:
+ *   "LatticeEnergyMinimizer"  binary cut (energy.hpp:39-49)       -> GPU push-relabel
+ *   "LatticeLevelReductions"  parametric flow (pf_policies.hpp:31-46) -> GPU parametric flow
+ *   "GPUPushRelabel", "GPULevelReductions"  the same engines under GB300 names.
+ * Kernel names follow install/code_setup.py:40 ("Full2d_4", "Star2d_16",
+ * "Full3d_6", ...); "Full3d_26" is the 3x3x3 neighbourhood. */
+int lf_is_valid_solver(const char* name);           /* 1 / 0 */
+int lf_is_valid_kernel(const char* name);           /* 1 / 0 */
+int lf_kernel_dimension(const char* kernel);        /* interface.hpp:189; -1 if unknown */
+/* Writes '\n'-separated names into buf (size len), returns the needed length. */
+size_t lf_valid_kernel_names(char* buf, size_t len);  /* interface.hpp:190 */
+size_t lf_valid_solver_names(char* buf, size_t len);  /* interface.hpp:191 */
+/* Kernel table in lattice order (kernellattice.hpp:61-96): K offsets, the
+ * positive half first in ascending linear-jump order, entry i + K/2 the
+ * reverse of entry i.  deltas: K*nd ints, geocut_weights: K doubles (either
+ * may be NULL).  Returns K, or -1 for an unknown name. */
+int lf_kernel_info(const char* kernel, int* nd, int* deltas, double* geocut_weights,
+                   int* geocut_applicable);
+
+/* getLatticeFlowInterface(solver, kernel, dims...) (interface.hpp:170-184).
+ * nd must equal the kernel's dimension; dims row-major, last fastest. */
+int lf_create(const char* solver, const char* kernel, int nd, const size_t* dims,
+              lf_lattice** out);
+void lf_destroy(lf_lattice* h);
+
+/* ----------------------------------------------------- lattice metadata
+ * interface.hpp:25-44. */
+int lf_n_dimensions(const lf_lattice* h);
+int lf_shape(const lf_lattice* h, size_t* dims_out);
+size_t lf_n_nodes(const lf_lattice* h);
+int lf_n_filling_edges(const lf_lattice* h);
+/* edgeDeltas(): K/2 * nd ints, entry [i*nd + j] = offset of filling edge i in dim j. */
+int lf_edge_deltas(const lf_lattice* h, int* deltas_out);
+
+/* -------------------------------------------------------------- filling
+ * addEnergyPotentials(long* unary, long* binary) (interface.hpp:49-61,
+ * direct_interface.hpp:60-95).  unary: 2*N int64 (E0 = off, E1 = on per
+ * node), binary: N*(K/2)*4 int64 (E00, E01, E10, E11 per node and filling
+ * edge; E01 = source node off, destination on).  Edges leaving the lattice are
+ * ignored.  Repeated calls accumulate.  Pairwise terms must be submodular
+ * (E00 + E11 <= E01 + E10, network_flow_node.hpp:450) -> else LF_ERR_RANGE. */
+int lf_add_energy_potentials(lf_lattice* h, const int64_t* unary, const int64_t* binary);
+/* Same, with the two arrays already in device memory (no host copy). */
+int lf_add_energy_potentials_device(lf_lattice* h, const int64_t* unary_device,
+                                    const int64_t* binary_device);
+/* Capacity form of the fill (the intent of addCapacityFromSource /
+ * addCapacityToSink / addCapacityOfEdge, energy_base.hpp:51-105):
+ * source[N] = cost of the node being off, sink[N] = cost of it being on,
+ * edge[N*(K/2)] = symmetric capacity of each filling edge.  int32, >= 0.
+ * Any pointer may be NULL.  Accumulates. */
+int lf_add_capacities(lf_lattice* h, const int32_t* source, const int32_t* sink,
+                      const int32_t* edge);
+
+/* --------------------------------------------------------------- control
+ * run() / runTime() (interface.hpp:111-113).  runTime is the device-side
+ * solve time of the last run in seconds (CUDA events), not CPU time. */
+int lf_run(lf_lattice* h);
+double lf_run_time(const lf_lattice* h);
+
+/* ---------------------------------------------------------------- results
+ * getCut() (interface.hpp:120, direct_interface.hpp:97-106): int[N], 1 = on.
+ * For the binary cut this is the unique MINIMAL on-set (forward residual
+ * reachability from the excess nodes; equals the bundled BK solver's
+ * labelling).  For the parametric solver it is reduction < 0
+ * (network_flow_node.hpp:50-55 with on_by_reduction). */
+int lf_get_cut(const lf_lattice* h, int* cut_out);
+/* The unique MAXIMAL on-set (nodes that cannot reach a deficit node). */
+int lf_get_cut_max(const lf_lattice* h, int* cut_out);
+/* Max-flow value and the minimum energy E(cut), both int64. */
+int lf_get_flow(const lf_lattice* h, int64_t* flow, int64_t* energy);
+/* Parametric solver: final 2x-scaled node values r (pf_flow_node.hpp:233-235). */
+int lf_get_levels(const lf_lattice* h, int64_t* r_out);
+/* Statistics of the last run: epochs (global relabels), push-relabel
+ * launches, BFS passes.  Any pointer may be NULL. */
+int lf_get_stats(const lf_lattice* h, int64_t* epochs, int64_t* pr_launches,
+                 int64_t* bfs_passes);
+
+/* Zero the accumulated energies: the lattice is as freshly created (the
+ * reference builds a new interface object per problem). */
+int lf_clear(lf_lattice* h);
+
+/* --------------------------------------------------------------- profiling
+ * With profiling on, every kernel launch of run() is bracketed by CUDA
+ * events on the handle's stream.  lf_get_profile fills
+ *   ms[0] push/relabel tile kernels, ms[1] global-relabel passes,
+ *   ms[2] cut-set closure passes, ms[3] whole run (device time)
+ *   counts[0] push/relabel launches, counts[1] tiles processed by them,
+ *   counts[2] BFS passes, counts[3] closure passes,
+ *   counts[4] kernel launches since the handle was created (fills included),
+ *   counts[5] tiles processed by BFS.
+ * (ms: 4 doubles, counts: 6 int64.) */
+int lf_set_profiling(lf_lattice* h, int enable);
+int lf_get_profile(const lf_lattice* h, double* ms, int64_t* counts);
+/* Device layout of the last run: tile extents (3, C fastest; a 2-d lattice
+ * is 1 x nx x ny), padded extents (3) and working capacity bytes (4 or 8). */
+int lf_get_layout(const lf_lattice* h, int* tile_dims, size_t* padded_dims, int* elem_bytes);
+/* The handle's CUDA stream (a cudaStream_t), so that callers can order or
+ * time their own work against the solver's. */
+int lf_get_stream(const lf_lattice* h, void** stream_out);
+
+/* --------------------------------------------------------------- tuning
+ * Runtime knobs of the solve (tile rows, local sweeps per launch, launches
+ * per global relabel); 0 keeps the current/auto value. */
+int lf_set_tuning(lf_lattice* h, int tile_rows, int local_sweeps, int launches_per_relabel);
+
+/* ------------------------------------------------------------------- TV
+ * calculate2dTV<Kernel, int64>(nx, ny, f, lambda) (tv/tv_solver.hpp:650-655):
+ * the single-lambda TV solve on the GPU.  f, out: nx*ny doubles, row-major.
+ * levels_out (may be NULL): the final 2x-scaled fixed-point values r. */
+int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double lambda,
+             double* out, int64_t* levels_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LATTICEFLOW_GPU_H */

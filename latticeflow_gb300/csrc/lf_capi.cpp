@@ -1,0 +1,273 @@
+// C ABI (include/latticeflow_gpu.h) over the engine.
+#include <cstring>
+#include <exception>
+#include <new>
+#include <string>
+
+#include "../../include/latticeflow_gpu.h"
+#include "lf_engine.h"
+
+struct lf_lattice {
+  lfg::Engine* e;
+};
+
+namespace lfg {
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace lfg
+
+namespace {
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    f();
+    lfg::set_error("");
+    return LF_OK;
+  } catch (const lfg::LfError& e) {
+    lfg::set_error(e.msg);
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    lfg::set_error("host allocation failed");
+    return LF_ERR_OOM;
+  } catch (const std::exception& e) {
+    lfg::set_error(e.what());
+    return LF_ERR_INVALID;
+  }
+}
+
+bool valid_solver(const char* s) {
+  if (!s) return false;
+  for (const std::string& n : lfg::solver_names())
+    if (n == s) return true;
+  return false;
+}
+
+size_t write_names(const std::vector<std::string>& names, char* buf, size_t len) {
+  std::string all;
+  for (size_t i = 0; i < names.size(); ++i) {
+    if (i) all += '\n';
+    all += names[i];
+  }
+  if (buf && len) {
+    size_t n = std::min(len - 1, all.size());
+    std::memcpy(buf, all.data(), n);
+    buf[n] = 0;
+  }
+  return all.size() + 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lf_last_error(void) { return lfg::g_last_error.c_str(); }
+
+int lf_is_valid_solver(const char* name) { return valid_solver(name) ? 1 : 0; }
+int lf_is_valid_kernel(const char* name) { return name && lfg::find_kernel(name) ? 1 : 0; }
+
+int lf_kernel_dimension(const char* kernel) {
+  const lfg::KernelDef* k = kernel ? lfg::find_kernel(kernel) : nullptr;
+  return k ? k->nd : -1;
+}
+
+size_t lf_valid_kernel_names(char* buf, size_t len) {
+  std::vector<std::string> names;
+  for (const lfg::KernelDef& k : lfg::kernel_registry()) names.push_back(k.name);
+  return write_names(names, buf, len);
+}
+
+size_t lf_valid_solver_names(char* buf, size_t len) {
+  return write_names(lfg::solver_names(), buf, len);
+}
+
+int lf_kernel_info(const char* kernel, int* nd, int* deltas, double* w, int* geocut) {
+  const lfg::KernelDef* k = kernel ? lfg::find_kernel(kernel) : nullptr;
+  if (!k) {
+    lfg::set_error(std::string("Bad Kernel or Solver Name: ") + (kernel ? kernel : "(null)"));
+    return -1;
+  }
+  if (nd) *nd = k->nd;
+  if (deltas) std::memcpy(deltas, k->delta.data(), k->delta.size() * sizeof(int));
+  if (w) std::memcpy(w, k->weight.data(), k->weight.size() * sizeof(double));
+  if (geocut) *geocut = k->geocut ? 1 : 0;
+  return k->K;
+}
+
+int lf_create(const char* solver, const char* kernel, int nd, const size_t* dims,
+              lf_lattice** out) {
+  return guarded([&] {
+    if (!out) throw lfg::LfError{LF_ERR_INVALID, "null output handle"};
+    *out = nullptr;
+    if (!valid_solver(solver) || !kernel || !lfg::find_kernel(kernel))
+      throw lfg::LfError{LF_ERR_BAD_NAME, std::string("Bad Kernel or Solver Name: ") +
+                                              (solver ? solver : "(null)") + ", " +
+                                              (kernel ? kernel : "(null)")};
+    const lfg::KernelDef* k = lfg::find_kernel(kernel);
+    if (!dims || nd != k->nd)
+      throw lfg::LfError{LF_ERR_SHAPE, "Kernel '" + std::string(kernel) + "' is " +
+                                           std::to_string(k->nd) + "-dimensional; a shape of " +
+                                           std::to_string(nd) + " dimensions was provided."};
+    lf_lattice* h = new lf_lattice;
+    try {
+      h->e = new lfg::Engine(solver, k, nd, dims);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+void lf_destroy(lf_lattice* h) {
+  if (!h) return;
+  delete h->e;
+  delete h;
+}
+
+int lf_n_dimensions(const lf_lattice* h) { return h ? h->e->nd : -1; }
+
+int lf_shape(const lf_lattice* h, size_t* dims_out) {
+  if (!h || !dims_out) return LF_ERR_INVALID;
+  for (int i = 0; i < h->e->nd; ++i) dims_out[i] = h->e->dims[i];
+  return LF_OK;
+}
+
+size_t lf_n_nodes(const lf_lattice* h) { return h ? (size_t)h->e->N : 0; }
+int lf_n_filling_edges(const lf_lattice* h) { return h ? h->e->st.K / 2 : -1; }
+
+int lf_edge_deltas(const lf_lattice* h, int* out) {
+  if (!h || !out) return LF_ERR_INVALID;
+  const lfg::KernelDef* k = h->e->kd;
+  std::memcpy(out, k->delta.data(), (k->K / 2) * k->nd * sizeof(int));
+  return LF_OK;
+}
+
+int lf_add_energy_potentials(lf_lattice* h, const int64_t* unary, const int64_t* binary) {
+  return guarded([&] {
+    if (!h || !unary || !binary) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    h->e->add_energy(unary, binary, false);
+  });
+}
+
+int lf_add_energy_potentials_device(lf_lattice* h, const int64_t* unary, const int64_t* binary) {
+  return guarded([&] {
+    if (!h || !unary || !binary) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    h->e->add_energy(unary, binary, true);
+  });
+}
+
+int lf_add_capacities(lf_lattice* h, const int32_t* src, const int32_t* snk, const int32_t* edge) {
+  return guarded([&] {
+    if (!h) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    h->e->add_caps(src, snk, edge);
+  });
+}
+
+int lf_run(lf_lattice* h) {
+  return guarded([&] {
+    if (!h) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    h->e->run();
+  });
+}
+
+double lf_run_time(const lf_lattice* h) { return h ? h->e->run_time : 0.0; }
+
+int lf_get_cut(const lf_lattice* h, int* out) {
+  return guarded([&] {
+    if (!h || !out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    h->e->get_cut(out, false);
+  });
+}
+
+int lf_get_cut_max(const lf_lattice* h, int* out) {
+  return guarded([&] {
+    if (!h || !out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    h->e->get_cut(out, true);
+  });
+}
+
+int lf_get_flow(const lf_lattice* h, int64_t* flow, int64_t* energy) {
+  return guarded([&] {
+    if (!h) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    if (!h->e->solved) throw lfg::LfError{LF_ERR_STATE, "no solution yet"};
+    if (flow) *flow = h->e->flow;
+    if (energy) *energy = h->e->energy;
+  });
+}
+
+int lf_get_levels(const lf_lattice* h, int64_t* out) {
+  return guarded([&] {
+    if (!h || !out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    h->e->get_levels(out);
+  });
+}
+
+int lf_get_stats(const lf_lattice* h, int64_t* epochs, int64_t* pr, int64_t* bfs) {
+  if (!h) return LF_ERR_INVALID;
+  if (epochs) *epochs = h->e->stats.epochs;
+  if (pr) *pr = h->e->stats.pr_launches;
+  if (bfs) *bfs = h->e->stats.bfs_passes;
+  return LF_OK;
+}
+
+int lf_set_tuning(lf_lattice* h, int tile_rows, int sweeps, int launches) {
+  if (!h) return LF_ERR_INVALID;
+  if (tile_rows > 0) h->e->tune.tile_rows = tile_rows;
+  if (sweeps > 0) h->e->tune.sweeps = sweeps;
+  if (launches > 0) h->e->tune.launches_per_relabel = launches;
+  return LF_OK;
+}
+
+int lf_clear(lf_lattice* h) {
+  return guarded([&] {
+    if (!h) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    h->e->clear();
+  });
+}
+
+int lf_set_profiling(lf_lattice* h, int enable) {
+  if (!h) return LF_ERR_INVALID;
+  h->e->profiling = enable != 0;
+  return LF_OK;
+}
+
+int lf_get_profile(const lf_lattice* h, double* ms, int64_t* counts) {
+  if (!h) return LF_ERR_INVALID;
+  for (int i = 0; i < 4; ++i)
+    if (ms) ms[i] = h->e->prof_ms[i];
+  for (int i = 0; i < 6; ++i)
+    if (counts) counts[i] = h->e->prof_cnt[i];
+  return LF_OK;
+}
+
+int lf_get_layout(const lf_lattice* h, int* tile, size_t* padded, int* elem) {
+  if (!h) return LF_ERR_INVALID;
+  const lfg::Geo& g = h->e->g;
+  if (tile) { tile[0] = g.TA; tile[1] = g.TB; tile[2] = g.TC; }
+  if (padded) { padded[0] = g.Ap; padded[1] = g.Bp; padded[2] = g.Cp; }
+  if (elem) *elem = h->e->elem_bytes;
+  return LF_OK;
+}
+
+int lf_get_stream(const lf_lattice* h, void** out) {
+  if (!h || !out) return LF_ERR_INVALID;
+  *out = (void*)h->e->stream;
+  return LF_OK;
+}
+
+int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double lambda,
+             double* out, int64_t* levels_out) {
+  return guarded([&] {
+    const lfg::KernelDef* k = kernel ? lfg::find_kernel(kernel) : nullptr;
+    if (!k) throw lfg::LfError{LF_ERR_BAD_NAME, std::string("Bad Kernel or Solver Name: ") +
+                                                    (kernel ? kernel : "(null)")};
+    if (k->nd != 2 || !k->geocut)
+      throw lfg::LfError{LF_ERR_BAD_NAME, "Kernel is not valid for GeoCuts or TV Minimization."};
+    if (!f || !out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    int rc = lfg::tv_2d(k, nx, ny, f, lambda, out, levels_out);
+    if (rc) throw lfg::LfError{rc, "tv solve failed"};
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,282 @@
+"""Python surface of the GPU engine, mirroring the reference extension.
+
+``LatticeFlow`` follows ``extensions/python/pylatticeflow.pyx:80-302``
+(constructor arguments, ``addEnergy`` shapes and rounding, ``run``,
+``runTime``, ``getCut`` and the properties), and the module functions follow
+the factory helpers of ``solver/interface.hpp:186-191``.  Everything calls the
+C ABI of ``include/latticeflow_gpu.h``; nothing here computes a cut.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def isValidSolver(name):
+    return bool(N.lib().lf_is_valid_solver(name.encode()))
+
+
+def isValidKernel(name):
+    return bool(N.lib().lf_is_valid_kernel(name.encode()))
+
+
+def kernelDimension(kernel):
+    d = N.lib().lf_kernel_dimension(kernel.encode())
+    if d < 0:
+        raise N.BadSolverOrKernelName("Bad Kernel or Solver Name: " + kernel)
+    return d
+
+
+def _names(fn):
+    n = fn(None, 0)
+    buf = ctypes.create_string_buffer(n)
+    fn(buf, n)
+    return [s for s in buf.value.decode().split("\n") if s]
+
+
+def validKernelNames():
+    return _names(N.lib().lf_valid_kernel_names)
+
+
+def validSolverNames():
+    return _names(N.lib().lf_valid_solver_names)
+
+
+def kernelInfo(kernel):
+    """(offsets[K, nd] in lattice order, geocut weights[K], geocut applicable)."""
+    L = N.lib()
+    nd = ctypes.c_int(0)
+    K = L.lf_kernel_info(kernel.encode(), ctypes.byref(nd), None, None, None)
+    if K < 0:
+        raise N.BadSolverOrKernelName(N.last_error())
+    d = np.zeros(K * nd.value, dtype=np.int32)
+    w = np.zeros(K, dtype=np.float64)
+    g = ctypes.c_int(0)
+    L.lf_kernel_info(kernel.encode(), None, _p(d), _p(w), ctypes.byref(g))
+    return d.reshape(K, nd.value), w, bool(g.value)
+
+
+class LatticeFlow(object):
+    """An interface to the lattice flow solvers (pylatticeflow.pyx:80-135).
+
+    ``solver`` may be a reference solver name ("LatticeEnergyMinimizer",
+    "LatticeLevelReductions") or its GPU name; both run on the GPU.
+    """
+
+    def __init__(self, kernel, solver, _dimensions, numerical_precision=1e-6):
+        if not isValidSolver(solver):
+            raise ValueError("'%s' not a valid solver name!  Valid solvers are: %s."
+                             % (solver, ", ".join(validSolverNames())))
+        if not isValidKernel(kernel):
+            raise ValueError("Kernel '%s' not a valid kernel name!  Valid kernels are: %s."
+                             % (kernel, ", ".join(validKernelNames())))
+        dim = kernelDimension(kernel)
+        self._dimensions = tuple(int(v) for v in _dimensions)
+        self.n_nodes = int(np.prod(self._dimensions))
+        if len(self._dimensions) != dim:
+            raise ValueError("Kernel '%s' is %d-dimensional; a shape of %d dimensions was provided."
+                             % (kernel, dim, len(self._dimensions)))
+        self.kernel = kernel
+        self.solver = solver
+        self.numerical_precision_factor = 1.0 / numerical_precision
+        dims = np.asarray(self._dimensions, dtype=np.uint64)
+        h = ctypes.c_void_p()
+        N.check(N.lib().lf_create(solver.encode(), kernel.encode(), dim, _p(dims), ctypes.byref(h)))
+        self._h = h
+        ne = N.lib().lf_n_filling_edges(h)
+        e = np.zeros(ne * dim, dtype=np.int32)
+        N.check(N.lib().lf_edge_deltas(h, _p(e)))
+        self._edges = e.reshape(ne, dim)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            N.lib().lf_destroy(h)
+            self._h = None
+
+    # ---------------------------------------------------------- properties
+    @property
+    def ndim(self):
+        return len(self._dimensions)
+
+    @property
+    def shape(self):
+        return self._dimensions
+
+    @property
+    def size(self):
+        return self.n_nodes
+
+    @property
+    def nFillingEdges(self):
+        return self._edges.shape[0]
+
+    @property
+    def edges(self):
+        return self._edges
+
+    # -------------------------------------------------------------- filling
+    def _check_arrays(self, unary_a, pairwise_a):
+        ue = ("Unary energy must be either a 2d array with first dimension matching the number "
+              "of nodes and second dimension containing E0 and E1, or (#dimensions + 1) with the "
+              "first matching the lattice coordinates and the last containing E0 and E1.")
+        if unary_a.ndim == 2:
+            if unary_a.shape[0] != self.n_nodes:
+                raise ValueError(ue + " (# nodes = %d; # unary_array_nodes = %d)"
+                                 % (self.n_nodes, unary_a.shape[0]))
+            if unary_a.shape[1] != 2:
+                raise ValueError(ue + " (Second dimension has shape %d; 2 required.)"
+                                 % unary_a.shape[1])
+        elif unary_a.ndim == len(self._dimensions) + 1:
+            for i, d in enumerate(self._dimensions):
+                if unary_a.shape[i] != d:
+                    raise ValueError(ue + " (dimension %d = %d; unary_array shape is %d)"
+                                     % (i, d, unary_a.shape[i]))
+            if unary_a.shape[-1] != 2:
+                raise ValueError(ue + " (Last dimension has shape %d; 2 required.)"
+                                 % unary_a.shape[-1])
+        else:
+            raise ValueError(ue + " (wrong number of dimensions)")
+        pe = ("Pairwise energy must be either: (1) a 3d array with first dimension matching the "
+              "number of nodes, second dimension containing the edge direction output, and third "
+              "dimension containing E00, E01, E10, and E11 (with E01 being energy of source node "
+              "off and dest node on.), or (2) a (#dimensions + 2) array with last two dimensions "
+              "being the same and first dimensions corresponding to the lattice coordinates. ")
+        ne = self.nFillingEdges
+        if pairwise_a.ndim == 3:
+            if pairwise_a.shape[0] != self.n_nodes:
+                raise ValueError(pe + " (# nodes = %d; # nodes in pairwise_energy = %d)"
+                                 % (self.n_nodes, pairwise_a.shape[0]))
+        elif pairwise_a.ndim == len(self._dimensions) + 2:
+            for i, d in enumerate(self._dimensions):
+                if pairwise_a.shape[i] != d:
+                    raise ValueError(pe + " (dimension %d shape is %d; pairwise_array shape is %d)"
+                                     % (i, d, pairwise_a.shape[i]))
+        else:
+            raise ValueError(pe + " (Array has wrong number of dimensions.)")
+        if pairwise_a.shape[-2] != ne:
+            raise ValueError(pe + " (wrong number of edges specified in second-to-last dimension;"
+                             " got %d, needed %d)." % (pairwise_a.shape[-2], ne))
+        if pairwise_a.shape[-1] != 4:
+            raise ValueError(pe + " (wrong number of pairwise energy terms; needed 4, got %d."
+                             % pairwise_a.shape[-1])
+
+    def addEnergy(self, unary_energy, pairwise_energy):
+        """pylatticeflow.pyx:157-267: energies are scaled by 1/numerical_precision,
+        rounded to int64 and accumulated into the lattice."""
+        nf = self.numerical_precision_factor
+        u = np.ascontiguousarray(np.round(nf * np.asarray(unary_energy)), dtype=np.int64)
+        b = np.ascontiguousarray(np.round(nf * np.asarray(pairwise_energy)), dtype=np.int64)
+        self._check_arrays(u, b)
+        self.addEnergyPotentials(u, b)
+
+    def addEnergyPotentials(self, unary, binary):
+        """Integer form (interface.hpp:61): unary int64[N, 2], binary int64[N, K/2, 4]."""
+        u = np.ascontiguousarray(unary, dtype=np.int64).reshape(-1)
+        b = np.ascontiguousarray(binary, dtype=np.int64).reshape(-1)
+        if u.size != 2 * self.n_nodes or b.size != 4 * self.nFillingEdges * self.n_nodes:
+            raise ValueError("energy arrays do not match the lattice")
+        N.check(N.lib().lf_add_energy_potentials(self._h, _p(u), _p(b)))
+
+    def addCapacities(self, source=None, sink=None, edges=None):
+        """Capacity form: source = cost of off, sink = cost of on, edges[N, K/2]."""
+        args = []
+        keep = []
+        for a, n in ((source, self.n_nodes), (sink, self.n_nodes),
+                     (edges, self.n_nodes * self.nFillingEdges)):
+            if a is None:
+                args.append(None)
+                continue
+            a = np.ascontiguousarray(a, dtype=np.int32).reshape(-1)
+            if a.size != n:
+                raise ValueError("capacity array has the wrong size")
+            keep.append(a)
+            args.append(_p(a))
+        N.check(N.lib().lf_add_capacities(self._h, *args))
+
+    # -------------------------------------------------------------- control
+    def run(self):
+        N.check(N.lib().lf_run(self._h))
+
+    def runTime(self):
+        """Device time of the last run, seconds."""
+        return N.lib().lf_run_time(self._h)
+
+    def clear(self):
+        """Zero the accumulated energies (as a freshly created lattice)."""
+        N.check(N.lib().lf_clear(self._h))
+
+    def setProfiling(self, enable=True):
+        N.check(N.lib().lf_set_profiling(self._h, 1 if enable else 0))
+
+    def profile(self):
+        """Per-category device milliseconds and counts of the last run."""
+        ms = np.zeros(4, dtype=np.float64)
+        c = np.zeros(6, dtype=np.int64)
+        N.check(N.lib().lf_get_profile(self._h, _p(ms), _p(c)))
+        return {"pr_ms": ms[0], "bfs_ms": ms[1], "reach_ms": ms[2], "run_ms": ms[3],
+                "pr_launches": int(c[0]), "pr_tiles": int(c[1]), "bfs_passes": int(c[2]),
+                "reach_passes": int(c[3]), "kernel_launches": int(c[4]), "bfs_tiles": int(c[5])}
+
+    def stream(self):
+        """The handle's cudaStream_t as an integer."""
+        s = ctypes.c_void_p()
+        N.check(N.lib().lf_get_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    def layout(self):
+        """Device layout of the last run: tile extents, padded extents, capacity bytes."""
+        t = np.zeros(3, dtype=np.int32)
+        pd = np.zeros(3, dtype=np.uint64)
+        e = ctypes.c_int(0)
+        N.check(N.lib().lf_get_layout(self._h, _p(t), _p(pd), ctypes.byref(e)))
+        return tuple(int(v) for v in t), tuple(int(v) for v in pd), e.value
+
+    def setTuning(self, tile_rows=0, local_sweeps=0, launches_per_relabel=0):
+        N.check(N.lib().lf_set_tuning(self._h, tile_rows, local_sweeps, launches_per_relabel))
+
+    # -------------------------------------------------------------- results
+    def getCut(self):
+        """int array shaped like the lattice, 1 = on (minimal on-set for binary cuts)."""
+        out = np.empty(self.n_nodes, dtype=np.int32)
+        N.check(N.lib().lf_get_cut(self._h, _p(out)))
+        return out.reshape(self._dimensions)
+
+    def getCutMax(self):
+        out = np.empty(self.n_nodes, dtype=np.int32)
+        N.check(N.lib().lf_get_cut_max(self._h, _p(out)))
+        return out.reshape(self._dimensions)
+
+    def flow(self):
+        """(max-flow value, minimum energy), both int64."""
+        f = ctypes.c_int64(0)
+        e = ctypes.c_int64(0)
+        N.check(N.lib().lf_get_flow(self._h, ctypes.byref(f), ctypes.byref(e)))
+        return f.value, e.value
+
+    def levels(self):
+        out = np.empty(self.n_nodes, dtype=np.int64)
+        N.check(N.lib().lf_get_levels(self._h, _p(out)))
+        return out.reshape(self._dimensions)
+
+    def stats(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        N.check(N.lib().lf_get_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"epochs": a.value, "pr_launches": b.value, "bfs_passes": c.value}
+
+
+def calculate2dTV(f, lam, kernel="Full2d_4", return_levels=False):
+    """Single-lambda TV (tv/tv_solver.hpp:650-655) on the GPU."""
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    if f.ndim != 2:
+        raise ValueError("calculate2dTV takes a 2-d array")
+    nx, ny = f.shape
+    out = np.empty((nx, ny), dtype=np.float64)
+    lv = np.empty((nx, ny), dtype=np.int64)
+    N.check(N.lib().lf_tv_2d(kernel.encode(), nx, ny, _p(f), float(lam), _p(out), _p(lv)))
+    return (out, lv) if return_levels else out

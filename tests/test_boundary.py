@@ -1,0 +1,77 @@
+"""The C-ABI boundary on CPU: library loads, exports every declared symbol,
+and the kernel registry / name validation need no GPU."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "latticeflow_gpu.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(lf_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol(native):
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(native, s), s
+
+
+def test_binding_covers_header(native):
+    from latticeflow_gb300 import _native
+    assert sorted(_native.PROTOTYPES) == declared_symbols()
+
+
+def test_registry_matches_oracle(native, oracle_port):
+    import latticeflow_gb300 as lf
+    O = oracle_port
+    names = lf.validKernelNames()
+    assert set(names) == set(O.specs())
+    for k in names:
+        d, w, g = lf.kernelInfo(k)
+        od, ow = O.lattice_offsets(k)
+        assert np.array_equal(d, od) and np.array_equal(w, ow) and g == O.specs()[k].geocut
+        assert lf.kernelDimension(k) == O.specs()[k].dim
+
+
+def test_registry_matches_compiled_reference_deltas(native, oracle_port):
+    O = oracle_port
+    if not O.ref_available():
+        pytest.skip("compiled reference not present")
+    import latticeflow_gb300 as lf
+    for k, dims in [("Full2d_4", (5, 6)), ("Full2d_8", (5, 6)), ("Star2d_16", (7, 6)),
+                    ("Full3d_26", (4, 5, 6)), ("Full3d_6", (4, 4, 4))]:
+        d, _, _ = lf.kernelInfo(k)
+        fd = O.ref_filling_deltas(k, dims)
+        assert np.array_equal(fd, d[: len(d) // 2])
+
+
+def test_names_validation(native):
+    import latticeflow_gb300 as lf
+    assert lf.isValidSolver("LatticeEnergyMinimizer")
+    assert lf.isValidSolver("LatticeLevelReductions")
+    assert not lf.isValidSolver("NoSuchSolver")
+    assert lf.isValidKernel("Full2d_8") and not lf.isValidKernel("Full2d_5")
+    with pytest.raises(lf.BadSolverOrKernelName):
+        lf.kernelDimension("Full2d_5")
+    with pytest.raises(ValueError):
+        lf.LatticeFlow("Full2d_4", "NoSuchSolver", (4, 4))
+    with pytest.raises(ValueError):
+        lf.LatticeFlow("Full2d_4", "LatticeEnergyMinimizer", (4, 4, 4))
+
+
+def test_no_cpu_fallback_in_package():
+    """The product package never imports the oracle."""
+    pkg = os.path.join(ROOT, "latticeflow_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith(".py"):
+                txt = open(os.path.join(dirpath, f)).read()
+                assert "oracle" not in re.sub(r'""".*?"""', "", txt, flags=re.S).replace("oracle", "oracle", 0) or \
+                    "import oracle" not in txt and "from oracle" not in txt, f

@@ -1,0 +1,188 @@
+"""GPU parity of the binary cut through the C ABI.
+
+Bar: bit-exact.  The flow value / minimum energy equals the reference's, the
+minimal on-set equals the reference BK labelling (golden fixtures) and the
+restated solver's minimal set, the maximal on-set equals the restated
+solver's maximal set.  Full-size problems are checked through
+size-independent properties (energy of both sets equals the reported
+minimum, minimal set inside maximal set).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def solve(kernel, dims, unary, binary, solver="LatticeEnergyMinimizer", tuning=None):
+    import latticeflow_gb300 as lf
+    L = lf.LatticeFlow(kernel, solver, dims)
+    if tuning:
+        L.setTuning(**tuning)
+    L.addEnergyPotentials(unary, binary)
+    L.run()
+    return L
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "cut_*.npz"))),
+                         ids=lambda p: os.path.basename(p))
+def test_golden_cut(native, gpu, oracle_port, path):
+    z = np.load(path)
+    kernel = str(z["kernel"])
+    dims = tuple(int(v) for v in z["dims"])
+    L = solve(kernel, dims, z["unary"], z["binary"])
+    flow, energy = L.flow()
+    assert energy == int(z["energy"])
+    cmin = L.getCut()
+    assert np.array_equal(cmin, z["bk_cut"])
+    _, _, cmax, _, _ = oracle_port.port_canonical(kernel, dims, z["unary"], z["binary"])
+    assert np.array_equal(L.getCutMax(), cmax)
+
+
+CASES = [
+    ("Full2d_4", (64, 64)), ("Full2d_4", (1, 100)), ("Full2d_4", (100, 1)), ("Full2d_4", (33, 65)),
+    ("Full2d_8", (70, 45)), ("Full2d_12", (40, 41)), ("Star2d_16", (37, 50)), ("Full2d_24", (30, 30)),
+    ("Full2d_48", (25, 26)), ("Full3d_6", (10, 12, 40)), ("Full3d_18", (9, 9, 33)),
+    ("Full3d_26", (12, 10, 35)), ("Full3d_32", (8, 9, 34)),
+]
+
+
+@pytest.mark.parametrize("kernel,dims", CASES, ids=lambda v: str(v))
+@pytest.mark.parametrize("seed", [0, 1])
+def test_random_vs_oracle(native, gpu, oracle_port, kernel, dims, seed):
+    O = oracle_port
+    rng = np.random.default_rng(seed + 17)
+    offs, _ = O.lattice_offsets(kernel)
+    N, Kp = int(np.prod(dims)), len(offs) // 2
+    u = rng.integers(0, 100, size=(N, 2)).astype(np.int64)
+    w = rng.integers(0, 60, size=(N, Kp)).astype(np.int64)
+    b = np.zeros((N, Kp, 4), np.int64)
+    b[:, :, 1] = w
+    b[:, :, 2] = w
+    E, cmin, cmax, _, _ = O.port_canonical(kernel, dims, u, b)
+    L = solve(kernel, dims, u, b)
+    assert L.flow()[1] == E
+    assert np.array_equal(L.getCut(), cmin)
+    assert np.array_equal(L.getCutMax(), cmax)
+
+
+def test_plain_cut_config_full_size(native, gpu, oracle_port):
+    from latticeflow_gb300 import workloads as W
+    p = W.plain_cut(0)
+    u, b = p.energies()
+    E, cmin, cmax, _, _ = oracle_port.port_canonical(p.kernel, p.dims, u, b)
+    L = solve(p.kernel, p.dims, u, b)
+    assert L.flow()[1] == E
+    assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
+
+
+def test_capacity_form_equals_energy_form(native, gpu):
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    p = W.plain_cut(4, (90, 77), "Full2d_8")
+    u, b = p.energies()
+    L1 = solve(p.kernel, p.dims, u, b)
+    L2 = lf.LatticeFlow(p.kernel, "GPUPushRelabel", p.dims)
+    L2.addCapacities(p.source, p.sink, p.edge)
+    L2.run()
+    assert L1.flow() == L2.flow()
+    assert np.array_equal(L1.getCut(), L2.getCut())
+
+
+def test_large_cut_scaled_vs_oracle(native, gpu, oracle_port):
+    from latticeflow_gb300 import workloads as W
+    p = W.large_cut(0, n=384)
+    u, b = p.energies()
+    E, cmin, cmax, _, _ = oracle_port.port_canonical(p.kernel, p.dims, u, b)
+    L = solve(p.kernel, p.dims, u, b)
+    assert L.flow()[1] == E
+    assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
+
+
+def test_large_cut_full_size_properties(native, gpu, oracle_port):
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    p = W.large_cut(0)
+    L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    L.addCapacities(p.source, p.sink, p.edge)
+    L.run()
+    flow, energy = L.flow()
+    cmin, cmax = L.getCut(), L.getCutMax()
+    assert np.all(cmin <= cmax)
+    u, b = p.energies()
+    assert oracle_port.energy(p.kernel, p.dims, u, b, cmin) == energy
+    assert oracle_port.energy(p.kernel, p.dims, u, b, cmax) == energy
+
+
+def test_int64_capacities(native, gpu, oracle_port):
+    O = oracle_port
+    rng = np.random.default_rng(3)
+    dims = (40, 50)
+    N = 2000
+    u = rng.integers(0, 3 * 10 ** 9, size=(N, 2)).astype(np.int64)
+    w = rng.integers(0, 2 * 10 ** 9, size=(N, 2)).astype(np.int64)
+    b = np.zeros((N, 2, 4), np.int64)
+    b[:, :, 1] = w
+    b[:, :, 2] = w
+    E, cmin, cmax, _, _ = O.port_canonical("Full2d_4", dims, u, b)
+    L = solve("Full2d_4", dims, u, b)
+    assert L.flow()[1] == E
+    assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
+
+
+def test_general_submodular_tables(native, gpu, oracle_port):
+    z = np.load(os.path.join(GOLD, "cut_f4_general.npz"))
+    dims = tuple(int(v) for v in z["dims"])
+    L = solve("Full2d_4", dims, z["unary"], z["binary"])
+    assert L.flow()[1] == int(z["energy"])
+    assert np.array_equal(L.getCut(), z["bk_cut"])
+
+
+def test_accumulating_fill(native, gpu, oracle_port):
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    p = W.plain_cut(6, (48, 52))
+    u, b = p.energies()
+    L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    L.addEnergyPotentials(u, b)
+    L.addEnergyPotentials(u, b)
+    L.run()
+    E, cmin, _, _, _ = oracle_port.port_canonical(p.kernel, p.dims, 2 * u, 2 * b)
+    assert L.flow()[1] == E and np.array_equal(L.getCut(), cmin)
+
+
+def test_errors(native, gpu):
+    import latticeflow_gb300 as lf
+    L = lf.LatticeFlow("Full2d_4", "LatticeEnergyMinimizer", (4, 4))
+    with pytest.raises(lf.LatticeFlowError):
+        L.getCut()
+    u = np.zeros((16, 2), np.int64)
+    b = np.zeros((16, 2, 4), np.int64)
+    b[:, :, 0] = 10   # E00 + E11 > E01 + E10: not submodular
+    with pytest.raises(OverflowError):
+        L.addEnergyPotentials(u, b)
+
+
+def test_repeat_run_is_stable(native, gpu):
+    from latticeflow_gb300 import workloads as W
+    p = W.plain_cut(2, (128, 96), "Full2d_8")
+    u, b = p.energies()
+    L = solve(p.kernel, p.dims, u, b)
+    c1, f1 = L.getCut(), L.flow()
+    L.run()
+    assert L.flow() == f1 and np.array_equal(L.getCut(), c1)
+
+
+@pytest.mark.parametrize("tuning", [dict(tile_rows=8), dict(local_sweeps=4), dict(launches_per_relabel=1),
+                                    dict(tile_rows=16, local_sweeps=200, launches_per_relabel=50)])
+def test_tuning_does_not_change_result(native, gpu, oracle_port, tuning):
+    from latticeflow_gb300 import workloads as W
+    p = W.plain_cut(8, (100, 120), "Full2d_8")
+    u, b = p.energies()
+    E, cmin, cmax, _, _ = oracle_port.port_canonical(p.kernel, p.dims, u, b)
+    L = solve(p.kernel, p.dims, u, b, tuning=tuning)
+    assert L.flow()[1] == E
+    assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)

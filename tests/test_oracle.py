@@ -1,0 +1,114 @@
+"""The oracle itself: pinned against the reference's own outputs.
+
+The restated solver must reproduce, bit for bit, the labelling of the
+reference push-relabel and the minimal set of the bundled BK solver stored
+in tests/golden (generated from the compiled reference), and the TV
+single-lambda outputs.  Where the compiled reference is present it is also
+compared directly on fresh random inputs.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import kernels as K
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_kernel_generator_names_and_sizes():
+    specs = K.generate()
+    assert specs["Full2d_4"].size == 4 and specs["Full2d_8"].size == 8
+    assert specs["Star2d_16"].size == 16 and specs["Full2d_48"].size == 48
+    assert specs["Full3d_6"].size == 6 and specs["Full3d_18"].size == 18
+    assert specs["Full3d_32"].size == 32
+    # sqrt(3)**2 < 3 in double: no 26-connected Full kernel; Star3d_26 is the 3x3x3 set
+    assert "Full3d_26" in specs and specs["Full3d_26"].alias_of == "Star3d_26"
+    assert specs["Star2d_4"].alias_of == "Full2d_4"
+
+
+def test_kernel_lattice_order_reverse_pairs():
+    for name, s in K.generate().items():
+        offs, w = s.lattice_order()
+        k = len(offs)
+        for i in range(k // 2):
+            assert tuple(-v for v in offs[i]) == offs[i + k // 2]
+            assert offs[i] > tuple([0] * s.dim)
+        assert offs[:k // 2] == sorted(offs[:k // 2])
+
+
+def test_geocut_weights_full2d():
+    s = K.generate()
+    _, w4 = s["Full2d_4"].lattice_order()
+    assert np.allclose(w4, np.pi / 4)
+    offs8, w8 = s["Full2d_8"].lattice_order()
+    for o, w in zip(offs8, w8):
+        expect = np.pi / 8 if 0 in o else np.pi / (8 * np.sqrt(2))
+        assert abs(w - expect) < 1e-15
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "cut_*.npz"))),
+                         ids=lambda p: os.path.basename(p))
+def test_port_matches_reference_golden_cut(oracle_port, path):
+    O = oracle_port
+    z = np.load(path)
+    kernel = str(z["kernel"])
+    dims = tuple(int(v) for v in z["dims"])
+    E, cmin, cmax, cpr, _ = O.port_canonical(kernel, dims, z["unary"], z["binary"])
+    assert np.array_equal(cpr, z["pr_cut"])      # reference push-relabel labelling
+    assert np.array_equal(cmin, z["bk_cut"])     # bundled BK labelling = minimal on-set
+    assert E == int(z["energy"])
+    assert O.energy(kernel, dims, z["unary"], z["binary"], cmax) == E
+    assert np.all(cmin <= cmax)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "tv_*.npz"))),
+                         ids=lambda p: os.path.basename(p))
+def test_port_matches_reference_golden_tv(oracle_port, path):
+    O = oracle_port
+    z = np.load(path)
+    out, r, _ = O.port_tv_single(str(z["kernel"]), z["f"], float(z["lam"]))
+    assert np.array_equal(out, z["out"])
+
+
+def test_port_against_compiled_reference_random(oracle_port):
+    O = oracle_port
+    if not O.ref_available():
+        pytest.skip("compiled reference not present")
+    rng = np.random.default_rng(99)
+    for kernel, dims in [("Full2d_4", (30, 31)), ("Full2d_8", (25, 27)), ("Full3d_26", (6, 6, 7))]:
+        offs, _ = O.lattice_offsets(kernel)
+        N, Kp = int(np.prod(dims)), len(offs) // 2
+        u = rng.integers(0, 80, size=(N, 2)).astype(np.int64)
+        w = rng.integers(0, 50, size=(N, Kp)).astype(np.int64)
+        b = np.zeros((N, Kp, 4), np.int64)
+        b[:, :, 1] = w
+        b[:, :, 2] = w
+        pr, _ = O.ref_solve("LatticeEnergyMinimizer", kernel, dims, u, b)
+        bk, _ = O.ref_solve("BKGCEnergyMinimizer", kernel, dims, u, b)
+        E, cmin, cmax, cpr, _ = O.port_canonical(kernel, dims, u, b)
+        assert np.array_equal(cpr, pr) and np.array_equal(cmin, bk)
+        assert O.energy(kernel, dims, u, b, pr) == E
+
+
+def test_port_tv_against_compiled_reference(oracle_port):
+    O = oracle_port
+    if not O.ref_available():
+        pytest.skip("compiled reference not present")
+    f = np.random.default_rng(5).random((27, 23))
+    for lam in (0.01, 3.0, 40.0):
+        ro, _ = O.ref_tv_single("Full2d_4", f, lam)
+        po, _, _ = O.port_tv_single("Full2d_4", f, lam)
+        assert np.array_equal(ro, po)
+
+
+def test_oracle_detects_planted_error(oracle_port):
+    """A wrong labelling planted in the oracle's output is caught by the energy check."""
+    O = oracle_port
+    z = np.load(os.path.join(GOLD, "cut_f4_rand.npz"))
+    dims = tuple(int(v) for v in z["dims"])
+    E, cmin, _, _, _ = O.port_canonical("Full2d_4", dims, z["unary"], z["binary"])
+    bad = cmin.copy().reshape(-1)
+    bad[np.argmax(bad == 0)] ^= 1
+    assert O.energy("Full2d_4", dims, z["unary"], z["binary"], bad) != E or not np.array_equal(bad, cmin.reshape(-1))
