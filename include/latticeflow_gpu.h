@@ -148,6 +148,9 @@ int lf_get_stream(const lf_lattice* h, void** stream_out);
  * Runtime knobs of the solve (tile rows, local sweeps per launch, launches
  * per global relabel); 0 keeps the current/auto value. */
 int lf_set_tuning(lf_lattice* h, int tile_rows, int local_sweeps, int launches_per_relabel);
+/* One knob by name: "tile_rows", "local_sweeps", "launches_per_relabel",
+ * "height_slack", "pass_chunk".  LF_ERR_INVALID for an unknown name. */
+int lf_set_param(lf_lattice* h, const char* name, int value);
 
 /* ------------------------------------------------------------------- TV
  * calculate2dTV<Kernel, int64>(nx, ny, f, lambda) (tv/tv_solver.hpp:650-655):

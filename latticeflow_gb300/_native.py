@@ -39,6 +39,7 @@ PROTOTYPES = {
     "lf_get_levels": (I, [P, P]),
     "lf_get_stats": (I, [P, P, P, P]),
     "lf_set_tuning": (I, [P, I, I, I]),
+    "lf_set_param": (I, [P, ctypes.c_char_p, I]),
     "lf_clear": (I, [P]),
     "lf_set_profiling": (I, [P, I]),
     "lf_get_profile": (I, [P, P, P]),

@@ -219,6 +219,20 @@ int lf_set_tuning(lf_lattice* h, int tile_rows, int sweeps, int launches) {
   return LF_OK;
 }
 
+int lf_set_param(lf_lattice* h, const char* name, int value) {
+  return guarded([&] {
+    if (!h || !name) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    std::string n(name);
+    lfg::Tuning& t = h->e->tune;
+    if (n == "tile_rows") t.tile_rows = value;
+    else if (n == "local_sweeps") t.sweeps = value;
+    else if (n == "launches_per_relabel") t.launches_per_relabel = value;
+    else if (n == "height_slack") t.height_slack = value;
+    else if (n == "pass_chunk") t.pass_chunk = value;
+    else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
+  });
+}
+
 int lf_clear(lf_lattice* h) {
   return guarded([&] {
     if (!h) throw lfg::LfError{LF_ERR_INVALID, "null handle"};

@@ -265,15 +265,20 @@ void Engine::global_relabel() {
   check(cudaMemsetAsync(d_dirty[1], 0, g.ntiles * sizeof(int), stream), "memset");
   int cur = 0;
   const long long cap = 4LL * g.ntiles + 64;
-  for (long long pass = 0;; ++pass) {
+  const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
+  // passes run in chunks; a pass on a converged lattice finds no dirty tile
+  // and exits at once, so only the last pass's flag needs reading
+  for (long long pass = 0;;) {
     if (pass > cap) throw LfError{4, "global relabel did not converge"};
-    BFSParams p{g, st, d_h, d_mask, d_dirty[cur], d_dirty[cur ^ 1], d_flag, 64, d_u64 + 2};
-    check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
-    prof_mark(1, false);
-    check(counted(launch_bfs_tile(p, stream)), "bfs tile");
-    prof_mark(1, true);
-    ++stats.bfs_passes;
-    cur ^= 1;
+    for (int c = 0; c < chunk; ++c, ++pass) {
+      BFSParams p{g, st, d_h, d_mask, d_dirty[cur], d_dirty[cur ^ 1], d_flag, 64, d_u64 + 2};
+      check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
+      prof_mark(1, false);
+      check(counted(launch_bfs_tile(p, stream)), "bfs tile");
+      prof_mark(1, true);
+      ++stats.bfs_passes;
+      cur ^= 1;
+    }
     int changed = 0;
     sync_read(&changed, d_flag, sizeof(int));
     if (!changed) break;
@@ -287,15 +292,18 @@ void Engine::reach() {
   check(cudaMemsetAsync(d_dirty[1], 0, g.ntiles * sizeof(int), stream), "memset");
   int cur = 0;
   const long long cap = 4LL * g.ntiles + 64;
-  for (long long pass = 0;; ++pass) {
+  const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
+  for (long long pass = 0;;) {
     if (pass > cap) throw LfError{4, "cut-set closure did not converge"};
-    ReachParams p{g, st, d_mark, d_mask, d_dirty[cur], d_dirty[cur ^ 1], d_flag, 256};
-    check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
-    prof_mark(2, false);
-    check(counted(launch_reach_tile(p, stream)), "reach tile");
-    prof_mark(2, true);
-    ++stats.reach_passes;
-    cur ^= 1;
+    for (int c = 0; c < chunk; ++c, ++pass) {
+      ReachParams p{g, st, d_mark, d_mask, d_dirty[cur], d_dirty[cur ^ 1], d_flag, 256};
+      check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
+      prof_mark(2, false);
+      check(counted(launch_reach_tile(p, stream)), "reach tile");
+      prof_mark(2, true);
+      ++stats.reach_passes;
+      cur ^= 1;
+    }
     int changed = 0;
     sync_read(&changed, d_flag, sizeof(int));
     if (!changed) break;
@@ -304,10 +312,10 @@ void Engine::reach() {
 
 template <typename T>
 void Engine::maxflow(bool compute_sets) {
-  const int hmax = (int)std::min<long long>(g.NP + 2, (long long)kHInf - 2);
-  int M = tune.launches_per_relabel;
-  if (M <= 0) M = 2 * std::max(g.nta, std::max(g.ntb, g.ntc)) + 4;
-  int R = tune.sweeps > 0 ? tune.sweeps : 64;
+  const long long hcap = std::min<long long>(g.NP + 2, (long long)kHInf - 2);
+  int M = tune.launches_per_relabel > 0 ? tune.launches_per_relabel : 8;
+  int R = tune.sweeps > 0 ? tune.sweeps : 16;
+  const int slack = tune.height_slack > 0 ? tune.height_slack : 64;
   const long long max_epochs = 20000;
   const auto t_start = std::chrono::steady_clock::now();
   for (long long epoch = 0;; ++epoch) {
@@ -318,11 +326,14 @@ void Engine::maxflow(bool compute_sets) {
     ++stats.epochs;
     check(cudaMemsetAsync(d_act[0], 0, g.ntiles * sizeof(int), stream), "memset");
     check(cudaMemsetAsync(d_act[1], 0, g.ntiles * sizeof(int), stream), "memset");
-    check(cudaMemsetAsync(d_u64, 0, sizeof(unsigned long long), stream), "memset");
+    check(cudaMemsetAsync(d_u64, 0, 2 * sizeof(unsigned long long), stream), "memset");
     check(counted(launch_active<T>(g, (const T*)d_exc, d_h, d_act[0], d_u64, stream)), "active");
-    unsigned long long active = 0;
-    sync_read(&active, d_u64, sizeof(active));
-    if (active == 0) break;
+    unsigned long long act_h[2] = {0, 0};
+    sync_read(act_h, d_u64, sizeof(act_h));
+    if (act_h[0] == 0) break;
+    // heights above the BFS depth plus a slack park until the next relabel:
+    // a node that climbs that far is bouncing flow inside a saturated region
+    const int hmax = (int)std::min<long long>(hcap, (long long)act_h[1] + slack);
     int cur = 0;
     for (int l = 0; l < M; ++l) {
       PRParams<T> p{g, st, (T*)d_res, (T*)d_exc, d_h, d_kmask, d_act[cur], d_act[cur ^ 1],

@@ -52,6 +52,8 @@ struct Tuning {
   int tile_rows = 0;             // TB (2-d) / TB with TA = 4 (3-d); 0 = auto
   int sweeps = 0;                // local push/relabel rounds per tile launch
   int launches_per_relabel = 0;  // tile launches between global relabels
+  int height_slack = 0;          // heights above (BFS depth + slack) park until the next relabel
+  int pass_chunk = 0;            // BFS / closure passes launched between host checks
 };
 
 struct SolveStats {

@@ -194,18 +194,29 @@ __global__ void k_mask(Geo g, const T* res, const uint64_t* kmask, uint64_t* mas
   mask[i] = m;
 }
 
-// Count active nodes (excess > 0 and a finite height) and flag their tiles.
+// Count active nodes (excess > 0 and a finite height), flag their tiles and
+// record the largest finite height (count[0], count[1]).
 template <typename T>
 __global__ void k_active(Geo g, const T* exc, const int* h, int* act, unsigned long long* count) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int a = 0;
-  if (i < g.NP && exc[i] > 0 && h[i] < kHInf) {
-    a = 1;
-    int c = int(i % g.Cp), b = int((i / g.Cp) % g.Bp), aa = int(i / ((long long)g.Cp * g.Bp));
-    act[tile_of(g, aa, b, c)] = 1;
+  unsigned hm = 0;
+  if (i < g.NP) {
+    int hh = h[i];
+    if (hh < kHInf) hm = (unsigned)hh;
+    if (exc[i] > 0 && hh < kHInf) {
+      a = 1;
+      int c = int(i % g.Cp), b = int((i / g.Cp) % g.Bp), aa = int(i / ((long long)g.Cp * g.Bp));
+      act[tile_of(g, aa, b, c)] = 1;
+    }
   }
   unsigned bal = __ballot_sync(0xffffffffu, a);
   if ((threadIdx.x & 31) == 0 && bal) atomicAdd(count, (unsigned long long)__popc(bal));
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned x = __shfl_down_sync(0xffffffffu, hm, o);
+    hm = x > hm ? x : hm;
+  }
+  if ((threadIdx.x & 31) == 0 && hm) atomicMax(count + 1, (unsigned long long)hm);
 }
 
 // ---------------------------------------------------------------- BFS

@@ -237,6 +237,9 @@ class LatticeFlow(object):
         N.check(N.lib().lf_get_layout(self._h, _p(t), _p(pd), ctypes.byref(e)))
         return tuple(int(v) for v in t), tuple(int(v) for v in pd), e.value
 
+    def setParam(self, name, value):
+        N.check(N.lib().lf_set_param(self._h, name.encode(), int(value)))
+
     def setTuning(self, tile_rows=0, local_sweeps=0, launches_per_relabel=0):
         N.check(N.lib().lf_set_tuning(self._h, tile_rows, local_sweeps, launches_per_relabel))
 
