@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--workload", default="large_cut",
                     choices=["large_cut", "plain_cut", "volume_cut"])
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--profile-run", action="store_true",
+                    help="only warm-up and timed device-resident solves (for ncu captures)")
     return ap.parse_args()
 
 
@@ -226,6 +228,12 @@ def run_ours(args):
 
     for _ in range(args.warmup):
         step_device()
+    if args.profile_run:
+        for _ in range(args.steps):
+            step_device()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_run": True, "flow": L.flow()[0]}))
+        return
     sampler = ClockSampler(local)
     sampler.start()
     ms, res, prof, launches = timed(step_device, args.steps, True)

@@ -313,9 +313,11 @@ void Engine::reach() {
 template <typename T>
 void Engine::maxflow(bool compute_sets) {
   const long long hcap = std::min<long long>(g.NP + 2, (long long)kHInf - 2);
-  int M = tune.launches_per_relabel > 0 ? tune.launches_per_relabel : 8;
-  int R = tune.sweeps > 0 ? tune.sweeps : 16;
-  const int slack = tune.height_slack > 0 ? tune.height_slack : 64;
+  // defaults from a sweep of (sweeps, launches, slack) on the 256^2 Full2d_4
+  // and 2048^2 Full2d_8 workloads
+  int M = tune.launches_per_relabel > 0 ? tune.launches_per_relabel : 4;
+  int R = tune.sweeps > 0 ? tune.sweeps : 4;
+  const int slack = tune.height_slack > 0 ? tune.height_slack : 16;
   const long long max_epochs = 20000;
   const auto t_start = std::chrono::steady_clock::now();
   for (long long epoch = 0;; ++epoch) {
