@@ -145,6 +145,8 @@ cudaError_t launch_pr_tile(const PRParams<T>& p, cudaStream_t s) {
     if (!attr_set) {                                                                      \
       cudaFuncSetAttribute(k_pr_tile<T, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                            227 * 1024);                                                   \
+      cudaFuncSetAttribute(k_pr_tile<T, KK>,                                              \
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);          \
       attr_set = true;                                                                    \
     }                                                                                     \
     k_pr_tile<T, KK><<<p.g.ntiles, threads, smem, s>>>(p);                                \
