@@ -202,8 +202,12 @@ void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device
     du = tu;
     db = tb;
   }
-  check(counted(launch_fill_energy(g, st, nd, N, du, db, d_exc64, d_cap64, d_c0, d_err, stream)),
-        "fill energy");
+  if (parametric)  // the reference's 2x-scaled reparametrisation (network_flow_node.hpp:420-485)
+    check(counted(launch_fill_energy_pf(g, st, nd, N, du, db, d_exc64, d_cap64, d_err, stream)),
+          "fill energy");
+  else
+    check(counted(launch_fill_energy(g, st, nd, N, du, db, d_exc64, d_cap64, d_c0, d_err, stream)),
+          "fill energy");
   if (tu) cudaFreeAsync(tu, stream);
   if (tb) cudaFreeAsync(tb, stream);
   int err = 0;
@@ -221,7 +225,7 @@ void Engine::add_caps(const int32_t* src, const int32_t* snk, const int32_t* edg
   if (src) { ds = buf; check(cudaMemcpyAsync(ds, src, nb, cudaMemcpyHostToDevice, stream), "memcpy"); }
   if (snk) { dt = buf + N; check(cudaMemcpyAsync(dt, snk, nb, cudaMemcpyHostToDevice, stream), "memcpy"); }
   if (edge) { de = buf + 2 * N; check(cudaMemcpyAsync(de, edge, eb, cudaMemcpyHostToDevice, stream), "memcpy"); }
-  check(counted(launch_fill_caps(g, st, nd, N, ds, dt, de, d_exc64, d_cap64, d_c0, d_err, stream)),
+  check(counted(launch_fill_caps(g, st, nd, N, ds, dt, de, d_exc64, d_cap64, d_c0, d_err, parametric ? 1 : 0, stream)),
         "fill caps");
   cudaFreeAsync(buf, stream);
   int err = 0;
@@ -259,7 +263,7 @@ void Engine::prepare_working(int elem) {
 
 template <typename T>
 void Engine::global_relabel() {
-  check(counted(launch_init_heights<T>(g, (const T*)d_exc, d_h, stream)), "init heights");
+  check(counted(launch_init_heights<T>(g, (const T*)d_exc, d_kmask, d_h, stream)), "init heights");
   check(counted(launch_mask<T>(g, st.K, (const T*)d_res, d_kmask, d_mask, stream)), "mask");
   check(cudaMemsetAsync(d_dirty[0], 0x01, g.ntiles * sizeof(int), stream), "memset");
   check(cudaMemsetAsync(d_dirty[1], 0, g.ntiles * sizeof(int), stream), "memset");

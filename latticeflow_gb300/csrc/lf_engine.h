@@ -22,10 +22,13 @@ cudaError_t launch_mask(const Geo& g, int K, const T* res, const uint64_t* kmask
 cudaError_t launch_fill_energy(const Geo& g, const Stencil& st, int nd, long long N,
                                const int64_t* u, const int64_t* b, long long* exc, long long* cap,
                                long long* c0, int* err, cudaStream_t s);
+cudaError_t launch_fill_energy_pf(const Geo& g, const Stencil& st, int nd, long long N,
+                                  const int64_t* u, const int64_t* b, long long* exc,
+                                  long long* cap, int* err, cudaStream_t s);
 cudaError_t launch_fill_caps(const Geo& g, const Stencil& st, int nd, long long N,
                              const int32_t* src, const int32_t* snk, const int32_t* edge,
                              long long* exc, long long* cap, long long* c0, int* err,
-                             cudaStream_t s);
+                             int pf2x, cudaStream_t s);
 cudaError_t launch_range_bound(const Geo& g, const Stencil& st, const long long* exc,
                                const long long* cap, unsigned long long* out, cudaStream_t s);
 template <typename T>
@@ -33,7 +36,8 @@ cudaError_t launch_convert(long long n, const long long* src, T* dst, cudaStream
 template <typename T>
 cudaError_t launch_sum_pos(long long n, const T* x, long long* out, cudaStream_t s);
 template <typename T>
-cudaError_t launch_init_heights(const Geo& g, const T* exc, int* h, cudaStream_t s);
+cudaError_t launch_init_heights(const Geo& g, const T* exc, const uint64_t* kmask, int* h,
+                                cudaStream_t s);
 template <typename T>
 cudaError_t launch_active(const Geo& g, const T* exc, const int* h, int* act,
                           unsigned long long* count, cudaStream_t s);

@@ -88,9 +88,12 @@ __global__ void k_fill_energy(Geo g, Stencil st, int nd, long long N, const int6
 }
 
 // Capacity form: source = cost off, sink = cost on, edge = symmetric capacity.
+// pf2x: the parametric solver's 2x-scaled form (reduction += 2 (sink - source),
+// alpha += 2 w both ways).
 __global__ void k_fill_caps(Geo g, Stencil st, int nd, long long N, const int32_t* src,
                             const int32_t* snk, const int32_t* edge, long long* exc,
-                            long long* cap, long long* c0sum, int* err) {
+                            long long* cap, long long* c0sum, int* err, int pf2x) {
+  const long long mul = pf2x ? 2 : 1;
   const int Kp = st.K / 2;
   long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long c0 = 0;
@@ -104,7 +107,7 @@ __global__ void k_fill_caps(Geo g, Stencil st, int nd, long long N, const int32_
     if (e == 0) {
       long long s = src ? src[b] : 0, t = snk ? snk[b] : 0;
       if (s < 0 || t < 0) atomicExch(err, 1);
-      if (s - t) atom_add(&exc[u], s - t);
+      if (s - t) atom_add(&exc[u], mul * (s - t));
       c0 += s;
     }
     if (edge) {
@@ -113,8 +116,8 @@ __global__ void k_fill_caps(Geo g, Stencil st, int nd, long long N, const int32_
       if (w < 0) atomicExch(err, 1);
       if (w > 0 && na >= 0 && na < g.A && nb >= 0 && nb < g.B && nc >= 0 && nc < g.C) {
         long long v = ((long long)na * g.Bp + nb) * g.Cp + nc;
-        atom_add(&cap[(long long)e * g.NP + u], w);
-        atom_add(&cap[(long long)st.rev[e] * g.NP + v], w);
+        atom_add(&cap[(long long)e * g.NP + u], mul * w);
+        atom_add(&cap[(long long)st.rev[e] * g.NP + v], mul * w);
       }
     }
   }
@@ -175,10 +178,14 @@ __global__ void k_sum_pos(long long n, const T* x, long long* out) {
 
 // ------------------------------------------------------------ epoch setup
 
+// Deficit nodes are the BFS roots.  With sections (kmask non-null) only
+// nodes whose bit 63 is set take part; the rest stay at kHInf.
 template <typename T>
-__global__ void k_init_heights(Geo g, const T* exc, int* h) {
+__global__ void k_init_heights(Geo g, const T* exc, const uint64_t* kmask, int* h) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < g.NP) h[i] = exc[i] < 0 ? 0 : kHInf;
+  if (i >= g.NP) return;
+  bool part = !kmask || (kmask[i] >> 63);
+  h[i] = (part && exc[i] < 0) ? 0 : kHInf;
 }
 
 // mask[i] bit k = res[k][i] > 0 (and the edge is inside the node's section)
@@ -432,10 +439,11 @@ cudaError_t launch_fill_energy(const Geo& g, const Stencil& st, int nd, long lon
 cudaError_t launch_fill_caps(const Geo& g, const Stencil& st, int nd, long long N,
                              const int32_t* src, const int32_t* snk, const int32_t* edge,
                              long long* exc, long long* cap, long long* c0, int* err,
-                             cudaStream_t s) {
+                             int pf2x, cudaStream_t s) {
   long long n = N * (st.K / 2);
   if (n > 0)
-    k_fill_caps<<<nblk(n, 256), 256, 0, s>>>(g, st, nd, N, src, snk, edge, exc, cap, c0, err);
+    k_fill_caps<<<nblk(n, 256), 256, 0, s>>>(g, st, nd, N, src, snk, edge, exc, cap, c0, err,
+                                             pf2x);
   return cudaGetLastError();
 }
 
@@ -464,13 +472,15 @@ template cudaError_t launch_sum_pos<long long>(long long, const long long*, long
                                                cudaStream_t);
 
 template <typename T>
-cudaError_t launch_init_heights(const Geo& g, const T* exc, int* h, cudaStream_t s) {
-  k_init_heights<T><<<nblk(g.NP, 256), 256, 0, s>>>(g, exc, h);
+cudaError_t launch_init_heights(const Geo& g, const T* exc, const uint64_t* kmask, int* h,
+                                cudaStream_t s) {
+  k_init_heights<T><<<nblk(g.NP, 256), 256, 0, s>>>(g, exc, kmask, h);
   return cudaGetLastError();
 }
-template cudaError_t launch_init_heights<int>(const Geo&, const int*, int*, cudaStream_t);
-template cudaError_t launch_init_heights<long long>(const Geo&, const long long*, int*,
-                                                    cudaStream_t);
+template cudaError_t launch_init_heights<int>(const Geo&, const int*, const uint64_t*, int*,
+                                              cudaStream_t);
+template cudaError_t launch_init_heights<long long>(const Geo&, const long long*,
+                                                    const uint64_t*, int*, cudaStream_t);
 
 template <typename T>
 cudaError_t launch_active(const Geo& g, const T* exc, const int* h, int* act,

@@ -1,7 +1,391 @@
-// Parametric flow / TV driver (filled in below).
+// Parametric flow (LatticeLevelReductions) and single-lambda TV on the GPU.
+//
+// Reference: ParametricFlowSolver::run (parametricflow/pf_solver.hpp:33-208)
+// processes a FIFO of node ranges; for each range it
+//   1. computes r_sum (128-bit), r_min, r_max of r = reduction + offset and
+//      stops when r_max - r_min <= 1, else moves the range's offset to
+//      r_new = ceil(double(r_sum) / count), minus one if that equals r_max
+//      (pf_flow_node.hpp:330-396);
+//   2. solves a key-restricted max-flow on the range (push_relabel.hpp:1360-1463);
+//   3. splits the range by the partition of every node and requeues both parts.
+// Ranges never exchange flow (edges between different keys are inert), so
+// every range of one queue generation is independent.  Here a whole
+// generation is one step: the statistics are reduced per section on the
+// device, the offsets are decided on the host with the reference's exact
+// integer / double rule, all sections are solved by ONE lattice-wide max-flow
+// with the cross-section edges masked out (kmask), and each section is split
+// by its maximal on-set (nodes that cannot reach a deficit node).
+//
+// Values use the reference's 2x-scaled representation (network_flow_node.hpp:
+// 420-485): exc = -(reduction) = -(r - offset).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 #include "lf_engine.h"
+#include "lf_tile_common.cuh"
 
 namespace lfg {
-void engine_run_parametric(Engine&) { throw LfError{8, "parametric solve not built yet"}; }
-int tv_2d(const KernelDef*, size_t, size_t, const double*, double, double*, int64_t*) { return 8; }
+
+namespace {
+
+inline int nblk(long long n, int t) { return int((n + t - 1) / t); }
+
+__device__ __forceinline__ void bounded_coords(const Geo& g, int nd, long long b, int& a, int& bb,
+                                               int& c) {
+  if (nd == 2) { a = 0; bb = int(b / g.C); c = int(b % g.C); }
+  else { c = int(b % g.C); bb = int((b / g.C) % g.B); a = int(b / ((long long)g.C * g.B)); }
+}
+
+// NodeFiller::addE1 / addE2 in 2x mode: reduction += 2(E1 - E0);
+// pairwise q1 = E10 - E00, q2 = E01 - E00, q12 = E00 + E11 - E01 - E10:
+// reduction1 += 2 q1 + q12, reduction2 += 2 q2 + q12, alpha both ways += -q12.
+__global__ void k_fill_energy_pf(Geo g, Stencil st, int nd, long long N, const int64_t* unary,
+                                 const int64_t* binary, long long* exc, long long* cap, int* err) {
+  const int Kp = st.K / 2;
+  long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= N * Kp) return;
+  long long b = tid / Kp;
+  int e = int(tid % Kp);
+  int a, bb, c;
+  bounded_coords(g, nd, b, a, bb, c);
+  long long u = ((long long)a * g.Bp + bb) * g.Cp + c;
+  if (e == 0) atom_add(&exc[u], -2LL * (unary[2 * b + 1] - unary[2 * b]));
+  int na = a + st.da[e], nb = bb + st.db[e], nc = c + st.dc[e];
+  if (na < 0 || na >= g.A || nb < 0 || nb >= g.B || nc < 0 || nc >= g.C) return;
+  long long v = ((long long)na * g.Bp + nb) * g.Cp + nc;
+  const int64_t* q = binary + (b * Kp + e) * 4;
+  long long q1 = q[2] - q[0], q2 = q[1] - q[0], q12 = q[0] + q[3] - q[1] - q[2];
+  if (q12 > 0) atomicExch(err, 1);
+  atom_add(&exc[u], -(2 * q1 + q12));
+  atom_add(&exc[v], -(2 * q2 + q12));
+  if (q12) {
+    atom_add(&cap[(long long)e * g.NP + u], -q12);
+    atom_add(&cap[(long long)st.rev[e] * g.NP + v], -q12);
+  }
+}
+
+// TV setup (tv/tv_solver.hpp:71-112): node value uf (fixed point) enters as
+// reduction 2 uf; every in-lattice edge of direction k gets 2 pwf[k].
+__global__ void k_fill_tv(Geo g, Stencil st, int nd, long long N, const int64_t* uf,
+                          const long long* pwf2, long long* exc, long long* cap) {
+  long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= N) return;
+  int a, bb, c;
+  bounded_coords(g, nd, b, a, bb, c);
+  long long u = ((long long)a * g.Bp + bb) * g.Cp + c;
+  exc[u] = -2LL * uf[b];
+  for (int k = 0; k < st.K; ++k) {
+    int na = a + st.da[k], nb = bb + st.db[k], nc = c + st.dc[k];
+    bool in = na >= 0 && na < g.A && nb >= 0 && nb < g.B && nc >= 0 && nc < g.C;
+    cap[(long long)k * g.NP + u] = in ? pwf2[k] : 0;
+  }
+}
+
+// Section of every in-lattice node = 0, padding = -1.
+__global__ void k_pf_init_keys(Geo g, int* key) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.NP) return;
+  int c = int(i % g.Cp), b = int((i / g.Cp) % g.Bp), a = int(i / ((long long)g.Cp * g.Bp));
+  key[i] = (a < g.A && b < g.B && c < g.C) ? 0 : -1;
+}
+
+// Per-section r statistics: 128-bit sum (lo, hi), count, min, max.
+// Lanes holding the same section are combined in the warp first.
+__global__ void k_pf_stats(long long NP, const int* key, const long long* exc,
+                           const long long* off, unsigned long long* lo, unsigned long long* hi,
+                           unsigned long long* cnt, long long* rmin, long long* rmax) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int s = -1;
+  long long r = 0;
+  if (i < NP) {
+    s = key[i];
+    if (s >= 0) r = off[s] - exc[i];
+  }
+  unsigned peers = __match_any_sync(0xffffffffu, s);
+  int leader = __ffs(peers) - 1;
+  int lane = threadIdx.x & 31;
+  long long sum = 0, mn = r, mx = r;
+  unsigned n = 0;
+  for (unsigned m = peers; m; m &= m - 1) {
+    int l = __ffs(m) - 1;
+    long long v = __shfl_sync(peers, r, l);
+    sum += v;
+    mn = v < mn ? v : mn;
+    mx = v > mx ? v : mx;
+    ++n;
+  }
+  if (s >= 0 && lane == leader) {
+    unsigned long long x = (unsigned long long)sum;
+    unsigned long long old = atomicAdd(&lo[s], x);
+    unsigned long long carry = (old + x) < old ? 1ull : 0ull;
+    unsigned long long hadd = (sum < 0 ? ~0ull : 0ull) + carry;
+    if (hadd) atomicAdd(&hi[s], hadd);
+    atomicAdd(&cnt[s], (unsigned long long)n);
+    atomicMin(&rmin[s], mn);
+    atomicMax(&rmax[s], mx);
+  }
+}
+
+// Sections marked finished fold their offset into the node (offset 0, as the
+// reference's final setOffset(0)) and leave the computation (key -2); the
+// others move their offset: exc += off_new - off_old.
+__global__ void k_pf_apply(long long NP, int* key, long long* exc, const long long* off_old,
+                           const long long* off_new, const unsigned char* finished) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NP) return;
+  int s = key[i];
+  if (s < 0) return;
+  if (finished[s]) {
+    exc[i] -= off_old[s];
+    key[i] = -2;
+  } else {
+    exc[i] += off_new[s] - off_old[s];
+  }
+}
+
+// bit k: neighbour k shares the node's (solving) section; bit 63: node solves.
+__global__ void k_pf_kmask(Geo g, Stencil st, const int* key, uint64_t* kmask) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.NP) return;
+  int s = key[i];
+  uint64_t m = 0;
+  if (s >= 0) {
+    m = 1ull << 63;
+    int c = int(i % g.Cp), b = int((i / g.Cp) % g.Bp), a = int(i / ((long long)g.Cp * g.Bp));
+    for (int k = 0; k < st.K; ++k) {
+      int na = a + st.da[k], nb = b + st.db[k], nc = c + st.dc[k];
+      if (na < 0 || na >= g.Ap || nb < 0 || nb >= g.Bp || nc < 0 || nc >= g.Cp) continue;
+      if (key[((long long)na * g.Bp + nb) * g.Cp + nc] == s) m |= 1ull << k;
+    }
+  }
+  kmask[i] = m;
+}
+
+// side = 1 for the maximal on-set (cannot reach a deficit), else 0.
+__global__ void k_pf_count(long long NP, const int* key, const int* h, unsigned long long* cnt2) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NP) return;
+  int s = key[i];
+  if (s < 0) return;
+  int side = h[i] >= kHInf ? 1 : 0;
+  atomicAdd(&cnt2[2 * s + side], 1ull);
+}
+
+__global__ void k_pf_remap(long long NP, int* key, const int* h, const int* child) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NP) return;
+  int s = key[i];
+  if (s < 0) return;
+  int side = h[i] >= kHInf ? 1 : 0;
+  key[i] = child[2 * s + side];
+}
+
+__global__ void k_pf_levels(Geo g, int nd, long long N, const long long* exc, int64_t* r) {
+  long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= N) return;
+  int a, bb, c;
+  bounded_coords(g, nd, b, a, bb, c);
+  r[b] = -exc[((long long)a * g.Bp + bb) * g.Cp + c];
+}
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  ~DevBuf() { if (p) cudaFree(p); }
+};
+
+}  // namespace
+
+cudaError_t launch_fill_energy_pf(const Geo& g, const Stencil& st, int nd, long long N,
+                                  const int64_t* u, const int64_t* b, long long* exc,
+                                  long long* cap, int* err, cudaStream_t s) {
+  long long n = N * (st.K / 2);
+  if (n > 0) k_fill_energy_pf<<<nblk(n, 256), 256, 0, s>>>(g, st, nd, N, u, b, exc, cap, err);
+  return cudaGetLastError();
+}
+
+// The parametric driver over an engine whose accumulators hold the 2x-scaled
+// reductions (exc64 = -reduction) and alphas (cap64).
+void engine_run_parametric(Engine& E) {
+  E.alloc_accumulators();
+  E.stats = SolveStats();
+  E.prepare_working(8);
+  const Geo& g = E.g;
+  cudaStream_t s = E.stream;
+  long long* exc = (long long*)E.d_exc;
+  const long long NP = g.NP;
+  const long long cap_sections = std::max<long long>(E.N, 1) + 1;
+
+  DevBuf<int> key;
+  DevBuf<long long> off_old, off_new, rmin, rmax;
+  DevBuf<unsigned long long> lo, hi, cnt, cnt2;
+  DevBuf<unsigned char> fin;
+  DevBuf<int> child;
+  E.check(cudaMalloc(&key.p, NP * sizeof(int)), "cudaMalloc");
+  E.check(cudaMalloc(&off_old.p, cap_sections * sizeof(long long)), "cudaMalloc");
+  E.check(cudaMalloc(&off_new.p, cap_sections * sizeof(long long)), "cudaMalloc");
+  E.check(cudaMalloc(&rmin.p, cap_sections * sizeof(long long)), "cudaMalloc");
+  E.check(cudaMalloc(&rmax.p, cap_sections * sizeof(long long)), "cudaMalloc");
+  E.check(cudaMalloc(&lo.p, cap_sections * sizeof(unsigned long long)), "cudaMalloc");
+  E.check(cudaMalloc(&hi.p, cap_sections * sizeof(unsigned long long)), "cudaMalloc");
+  E.check(cudaMalloc(&cnt.p, cap_sections * sizeof(unsigned long long)), "cudaMalloc");
+  E.check(cudaMalloc(&cnt2.p, 2 * cap_sections * sizeof(unsigned long long)), "cudaMalloc");
+  E.check(cudaMalloc(&fin.p, cap_sections), "cudaMalloc");
+  E.check(cudaMalloc(&child.p, 2 * cap_sections * sizeof(int)), "cudaMalloc");
+  if (!E.d_kmask) E.check(cudaMalloc(&E.d_kmask, NP * sizeof(uint64_t)), "cudaMalloc kmask");
+
+  E.check(cudaEventRecord(E.ev0, s), "event");
+  k_pf_init_keys<<<nblk(NP, 256), 256, 0, s>>>(g, key.p);
+  E.check(E.counted(cudaGetLastError()), "init keys");
+  E.check(cudaMemsetAsync(off_old.p, 0, sizeof(long long), s), "memset");
+
+  long long S = E.N > 0 ? 1 : 0;  // sections of the current generation, ids 0..S-1
+  std::vector<unsigned long long> h_lo, h_hi, h_cnt, h_cnt2;
+  std::vector<long long> h_min, h_max, h_off, h_new;
+  std::vector<unsigned char> h_fin;
+  std::vector<int> h_child;
+  const long long max_rounds = 100000;
+  for (long long round = 0; S > 0; ++round) {
+    if (round > max_rounds) throw LfError{4, "parametric flow did not converge"};
+    // 1. statistics of every section
+    E.check(cudaMemsetAsync(lo.p, 0, S * 8, s), "memset");
+    E.check(cudaMemsetAsync(hi.p, 0, S * 8, s), "memset");
+    E.check(cudaMemsetAsync(cnt.p, 0, S * 8, s), "memset");
+    E.check(cudaMemsetAsync(rmin.p, 0x7f, S * 8, s), "memset");
+    E.check(cudaMemsetAsync(rmax.p, 0x80, S * 8, s), "memset");
+    k_pf_stats<<<nblk(NP, 256), 256, 0, s>>>(NP, key.p, exc, off_old.p, lo.p, hi.p, cnt.p,
+                                             rmin.p, rmax.p);
+    E.check(E.counted(cudaGetLastError()), "pf stats");
+    h_lo.resize(S); h_hi.resize(S); h_cnt.resize(S); h_min.resize(S); h_max.resize(S);
+    h_off.resize(S); h_new.resize(S); h_fin.assign(S, 0);
+    E.check(cudaMemcpyAsync(h_lo.data(), lo.p, S * 8, cudaMemcpyDeviceToHost, s), "memcpy");
+    E.check(cudaMemcpyAsync(h_hi.data(), hi.p, S * 8, cudaMemcpyDeviceToHost, s), "memcpy");
+    E.check(cudaMemcpyAsync(h_cnt.data(), cnt.p, S * 8, cudaMemcpyDeviceToHost, s), "memcpy");
+    E.check(cudaMemcpyAsync(h_min.data(), rmin.p, S * 8, cudaMemcpyDeviceToHost, s), "memcpy");
+    E.check(cudaMemcpyAsync(h_max.data(), rmax.p, S * 8, cudaMemcpyDeviceToHost, s), "memcpy");
+    E.check(cudaMemcpyAsync(h_off.data(), off_old.p, S * 8, cudaMemcpyDeviceToHost, s), "memcpy");
+    E.check(cudaStreamSynchronize(s), "sync");
+    // 2. the reference's offset rule, exactly (pf_flow_node.hpp:364-374)
+    long long solving = 0;
+    for (long long i = 0; i < S; ++i) {
+      if (h_max[i] - h_min[i] <= 1) { h_fin[i] = 1; h_new[i] = h_off[i]; continue; }
+      __int128 sum = (__int128)(((unsigned __int128)h_hi[i] << 64) | h_lo[i]);
+      double count = double(h_cnt[i]);
+      long long r_new = (long long)std::ceil(double(sum) / count);
+      if (r_new == h_max[i]) --r_new;
+      h_new[i] = r_new;
+      ++solving;
+    }
+    E.check(cudaMemcpyAsync(off_new.p, h_new.data(), S * 8, cudaMemcpyHostToDevice, s), "memcpy");
+    E.check(cudaMemcpyAsync(fin.p, h_fin.data(), S, cudaMemcpyHostToDevice, s), "memcpy");
+    k_pf_apply<<<nblk(NP, 256), 256, 0, s>>>(NP, key.p, exc, off_old.p, off_new.p, fin.p);
+    E.check(E.counted(cudaGetLastError()), "pf apply");
+    if (solving == 0) { E.check(cudaStreamSynchronize(s), "sync"); break; }
+    // 3. one max-flow for every solving section
+    k_pf_kmask<<<nblk(NP, 256), 256, 0, s>>>(g, E.st, key.p, E.d_kmask);
+    E.check(E.counted(cudaGetLastError()), "pf kmask");
+    E.maxflow<long long>(false);
+    // 4. split each section by its maximal on-set
+    E.check(cudaMemsetAsync(cnt2.p, 0, 2 * S * 8, s), "memset");
+    k_pf_count<<<nblk(NP, 256), 256, 0, s>>>(NP, key.p, E.d_h, cnt2.p);
+    E.check(E.counted(cudaGetLastError()), "pf count");
+    h_cnt2.resize(2 * S);
+    E.check(cudaMemcpyAsync(h_cnt2.data(), cnt2.p, 2 * S * 8, cudaMemcpyDeviceToHost, s), "memcpy");
+    E.check(cudaStreamSynchronize(s), "sync");
+    h_child.assign(2 * S, -1);
+    std::vector<long long> next_off;
+    long long S2 = 0;
+    for (long long i = 0; i < S; ++i) {
+      if (h_fin[i]) continue;
+      for (int side = 0; side < 2; ++side)
+        if (h_cnt2[2 * i + side] > 0) {
+          h_child[2 * i + side] = int(S2++);
+          next_off.push_back(h_new[i]);
+        }
+    }
+    if (S2 > cap_sections) throw LfError{4, "section count overflow"};
+    E.check(cudaMemcpyAsync(child.p, h_child.data(), 2 * S * sizeof(int), cudaMemcpyHostToDevice, s), "memcpy");
+    k_pf_remap<<<nblk(NP, 256), 256, 0, s>>>(NP, key.p, E.d_h, child.p);
+    E.check(E.counted(cudaGetLastError()), "pf remap");
+    if (S2 > 0)
+      E.check(cudaMemcpyAsync(off_old.p, next_off.data(), S2 * 8, cudaMemcpyHostToDevice, s), "memcpy");
+    E.check(cudaStreamSynchronize(s), "sync");
+    S = S2;
+    ++E.stats.epochs;  // generations are reported as epochs for the parametric solver
+  }
+  E.check(cudaEventRecord(E.ev1, s), "event");
+  E.levels_host.assign((size_t)E.N, 0);
+  if (E.N > 0) {
+    DevBuf<int64_t> r;
+    E.check(cudaMalloc(&r.p, E.N * sizeof(int64_t)), "cudaMalloc");
+    k_pf_levels<<<nblk(E.N, 256), 256, 0, s>>>(g, E.nd, E.N, exc, r.p);
+    E.check(E.counted(cudaGetLastError()), "pf levels");
+    E.check(cudaMemcpyAsync(E.levels_host.data(), r.p, E.N * 8, cudaMemcpyDeviceToHost, s), "memcpy");
+    E.check(cudaStreamSynchronize(s), "sync");
+  }
+  float ms = 0;
+  cudaEventElapsedTime(&ms, E.ev0, E.ev1);
+  E.run_time = ms * 1e-3;
+  E.prof_ms[3] = ms;
+  cudaFree(E.d_kmask);
+  E.d_kmask = nullptr;
+  E.solved = true;
+}
+
+// calculate2dTV<Kernel, int64>(nx, ny, f, lambda)  (tv/tv_solver.hpp:650-655)
+int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lambda, double* out,
+          int64_t* levels_out) {
+  const int nbits = 40;  // n_bits_function_precision for int64 (pf_flow_node.hpp:103-115)
+  const double fscale = double(int64_t(1) << nbits);
+  const size_t N = nx * ny;
+  if (N == 0) return 0;
+  // setup (tv_solver.hpp:71-112), sequential double arithmetic as the reference
+  double v_min = f[0], v_max = f[0], v_sum = f[0];
+  for (size_t i = 1; i < N; ++i) {
+    v_min = std::min(v_min, f[i]);
+    v_max = std::max(v_max, f[i]);
+    v_sum += f[i];
+  }
+  const double mean = v_sum / double(N);
+  v_min -= mean;
+  v_max -= mean;
+  const double scale = 2 * std::max(v_max, -v_min);
+  const double max_lambda = std::max(lambda, 1e-8);
+  std::vector<int64_t> uf(N);
+  for (size_t i = 0; i < N; ++i) uf[i] = int64_t(std::round((0.5 + (f[i] - mean) / scale) * fscale));
+  const double gsv = 0.5 / (scale * max_lambda);
+  std::vector<long long> pwf2(kd->K);
+  for (int k = 0; k < kd->K; ++k)
+    pwf2[k] = 2LL * (long long)std::round((gsv * kd->weight[k]) / scale * fscale);
+
+  size_t dims[2] = {nx, ny};
+  Engine E("GPULevelReductions", kd, 2, dims);
+  E.alloc_accumulators();
+  DevBuf<int64_t> d_uf;
+  DevBuf<long long> d_pwf;
+  E.check(cudaMalloc(&d_uf.p, N * sizeof(int64_t)), "cudaMalloc");
+  E.check(cudaMalloc(&d_pwf.p, kd->K * sizeof(long long)), "cudaMalloc");
+  E.check(cudaMemcpyAsync(d_uf.p, uf.data(), N * 8, cudaMemcpyHostToDevice, E.stream), "memcpy");
+  E.check(cudaMemcpyAsync(d_pwf.p, pwf2.data(), kd->K * 8, cudaMemcpyHostToDevice, E.stream), "memcpy");
+  k_fill_tv<<<nblk((long long)N, 256), 256, 0, E.stream>>>(E.g, E.st, 2, (long long)N, d_uf.p,
+                                                           d_pwf.p, E.d_exc64, E.d_cap64);
+  E.check(cudaGetLastError(), "fill tv");
+  engine_run_parametric(E);
+  // output (tv_solver.hpp:159-175): value of r/2 in the fixed point, mean removed
+  std::vector<double> R(N);
+  double sum = 0;
+  for (size_t i = 0; i < N; ++i) {
+    int64_t r = E.levels_host[i];
+    if (levels_out) levels_out[i] = r;
+    double x = double(r / 2) / fscale;
+    double v = (x - 0.5) * scale + mean;
+    R[i] = v;
+    sum += v;
+  }
+  for (size_t i = 0; i < N; ++i) out[i] = (R[i] - sum / double(N)) * scale + mean;
+  return 0;
+}
+
 }  // namespace lfg

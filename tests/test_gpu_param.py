@@ -1,0 +1,89 @@
+"""Parametric flow and single-lambda TV on the GPU, against the oracle.
+
+The reference's final 2x-scaled values r are a deterministic function of the
+level sets up to the distribution of the rounding remainder inside a level
+set, which depends on the order of pushes; the GPU's values are therefore
+compared with a tolerance of R_TOL raw units, and the double outputs of the
+TV solver with a relative tolerance of OUT_RTOL (1 raw unit is 2^-41 of the
+function range).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+R_TOL = 2
+OUT_RTOL = 1e-9
+
+
+def _close_out(a, b):
+    scale = max(1.0, float(np.abs(b).max()))
+    return float(np.abs(a - b).max()) <= OUT_RTOL * scale
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "tv_*.npz"))),
+                         ids=lambda p: os.path.basename(p))
+def test_tv_golden(native, gpu, oracle_port, path):
+    import latticeflow_gb300 as lf
+    z = np.load(path)
+    kernel = str(z["kernel"])
+    out, lv = lf.calculate2dTV(z["f"], float(z["lam"]), kernel=kernel, return_levels=True)
+    _, r, _ = oracle_port.port_tv_single(kernel, z["f"], float(z["lam"]))
+    dr = int(np.abs(lv - r).max())
+    print(os.path.basename(path), "max |dr| =", dr, "max |dout| =", float(np.abs(out - z["out"]).max()))
+    assert dr <= R_TOL
+    assert _close_out(out, z["out"])
+
+
+@pytest.mark.parametrize("lam", [0.002, 0.3, 5.0, 100.0])
+def test_tv_image_vs_oracle(native, gpu, oracle_port, lam):
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    f = W.tv_image(1, n=96, polygons=6)
+    out, lv = lf.calculate2dTV(f, lam, return_levels=True)
+    ref, r, _ = oracle_port.port_tv_single("Full2d_4", f, lam)
+    dr = int(np.abs(lv - r).max())
+    print("lam", lam, "max |dr| =", dr, "levels", len(np.unique(r)))
+    assert dr <= R_TOL
+    assert _close_out(out, ref)
+
+
+def test_tv_ragged_and_tiny(native, gpu, oracle_port):
+    import latticeflow_gb300 as lf
+    rng = np.random.default_rng(4)
+    for shape in [(1, 1), (1, 7), (5, 1), (33, 65), (70, 3)]:
+        f = rng.random(shape)
+        out, lv = lf.calculate2dTV(f, 20.0, return_levels=True)
+        ref, r, _ = oracle_port.port_tv_single("Full2d_4", f, 20.0)
+        assert int(np.abs(lv - r).max()) <= R_TOL, shape
+        assert _close_out(out, ref), shape
+
+
+@pytest.mark.parametrize("kernel,dims", [("Full2d_4", (40, 37)), ("Full2d_8", (31, 29)),
+                                         ("Full3d_6", (9, 10, 33))])
+def test_level_reductions_vs_oracle(native, gpu, oracle_port, kernel, dims):
+    """LatticeLevelReductions through the generic interface (pf_policies.hpp:31-46)."""
+    import latticeflow_gb300 as lf
+    O = oracle_port
+    rng = np.random.default_rng(11)
+    offs, _ = O.lattice_offsets(kernel)
+    N, Kp = int(np.prod(dims)), len(offs) // 2
+    u = rng.integers(0, 1000, size=(N, 2)).astype(np.int64)
+    w = rng.integers(0, 300, size=(N, Kp)).astype(np.int64)
+    b = np.zeros((N, Kp, 4), np.int64)
+    b[:, :, 1] = w
+    b[:, :, 2] = w
+    r_ref, cut_ref, _ = O.port_pf(kernel, dims, u, b)
+    L = lf.LatticeFlow(kernel, "LatticeLevelReductions", dims)
+    L.addEnergyPotentials(u, b)
+    L.run()
+    r = L.levels()
+    dr = int(np.abs(r - r_ref).max())
+    print(kernel, "max |dr| =", dr, "levels", len(np.unique(r_ref)))
+    assert dr <= R_TOL
+    assert int(r.sum()) == int(r_ref.sum())      # total is exact
+    sure = np.abs(r_ref) > R_TOL
+    assert np.array_equal(L.getCut()[sure], cut_ref[sure])
