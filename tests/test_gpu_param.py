@@ -3,7 +3,7 @@
 The reference's final 2x-scaled values r are a deterministic function of the
 level sets up to the distribution of the rounding remainder inside a level
 set, which depends on the order of pushes; the GPU's values are therefore
-compared with a tolerance of R_TOL raw units, and the double outputs of the
+compared with a tolerance of R_TOL = 1 raw unit, and the double outputs of the
 TV solver with a relative tolerance of OUT_RTOL (1 raw unit is 2^-41 of the
 function range).
 """
@@ -15,7 +15,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
-R_TOL = 2
+R_TOL = 1
 OUT_RTOL = 1e-9
 
 
