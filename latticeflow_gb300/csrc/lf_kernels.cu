@@ -1,25 +1,10 @@
-// CUDA kernels of the lattice max-flow engine (sm_103a).
-//
-// The reference solves one lattice with a sequential highest-label
-// push-relabel (network_flow/push_relabel.hpp:1069-1278).  Here the same
-// preflow problem is solved by synchronous tile sweeps:
-//   * k_pr_tile     stages one tile (all residual planes, excess, heights with
-//                   a halo) in shared memory and runs up to `sweeps` local
-//                   push / relabel rounds; flow pushed across the tile edge is
-//                   delivered to the neighbour tile with global atomics at the
-//                   end of the launch.
-//   * k_bfs_tile    global relabel: exact distance to the nearest deficit
-//                   node along residual edges (the reference's hotStart BFS,
-//                   push_relabel.hpp:306-415), tile-local wavefronts repeated
-//                   until no tile changes.  Nodes left at kHInf cannot reach a
-//                   deficit: the reference flips exactly those
-//                   (push_relabel.hpp:394-402, gap flip :692-711).
-//   * k_reach_tile  forward residual closure of the excess nodes (the unique
-//                   minimal on-set).
-// All capacities are integers; results are exact.
+// Per-lattice element kernels: energy / capacity fill, range bound, type
+// conversion, reductions and cut extraction.  The solve itself runs on the
+// pool kernels (lf_pool_tile.cuh, lf_pool.cu).
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "lf_pool_runner.h"
 #include "lf_tile_common.cuh"
 
 namespace lfg {
@@ -176,180 +161,6 @@ __global__ void k_sum_pos(long long n, const T* x, long long* out) {
   if ((threadIdx.x & 31) == 0 && v) atom_add(out, v);
 }
 
-// ------------------------------------------------------------ epoch setup
-
-// Deficit nodes are the BFS roots.  With sections (kmask non-null) only
-// nodes whose bit 63 is set take part; the rest stay at kHInf.
-template <typename T>
-__global__ void k_init_heights(Geo g, const T* exc, const uint64_t* kmask, int* h) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= g.NP) return;
-  bool part = !kmask || (kmask[i] >> 63);
-  h[i] = (part && exc[i] < 0) ? 0 : kHInf;
-}
-
-// mask[i] bit k = res[k][i] > 0 (and the edge is inside the node's section)
-template <typename T, int K>
-__global__ void k_mask(Geo g, const T* res, const uint64_t* kmask, uint64_t* mask) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= g.NP) return;
-  uint64_t m = 0;
-#pragma unroll
-  for (int k = 0; k < K; ++k)
-    if (res[(long long)k * g.NP + i] > 0) m |= 1ull << k;
-  if (kmask) m &= kmask[i];
-  mask[i] = m;
-}
-
-// Count active nodes (excess > 0 and a finite height), flag their tiles and
-// record the largest finite height (count[0], count[1]).
-template <typename T>
-__global__ void k_active(Geo g, const T* exc, const int* h, int* act, unsigned long long* count) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  int a = 0;
-  unsigned hm = 0;
-  if (i < g.NP) {
-    int hh = h[i];
-    if (hh < kHInf) hm = (unsigned)hh;
-    if (exc[i] > 0 && hh < kHInf) {
-      a = 1;
-      int c = int(i % g.Cp), b = int((i / g.Cp) % g.Bp), aa = int(i / ((long long)g.Cp * g.Bp));
-      act[tile_of(g, aa, b, c)] = 1;
-    }
-  }
-  unsigned bal = __ballot_sync(0xffffffffu, a);
-  if ((threadIdx.x & 31) == 0 && bal) atomicAdd(count, (unsigned long long)__popc(bal));
-  for (int o = 16; o > 0; o >>= 1) {
-    unsigned x = __shfl_down_sync(0xffffffffu, hm, o);
-    hm = x > hm ? x : hm;
-  }
-  if ((threadIdx.x & 31) == 0 && hm) atomicMax(count + 1, (unsigned long long)hm);
-}
-
-// ---------------------------------------------------------------- BFS
-
-template <int K>
-__global__ void __launch_bounds__(1024) k_bfs_tile(BFSParams p) {
-  const int tile = blockIdx.x;
-  if (!p.dirty_cur[tile]) return;
-  extern __shared__ __align__(16) unsigned char smem[];
-  const Geo& g = p.g;
-  const TileCtx x = tile_ctx(g, p.st, tile);
-  int* s_h = reinterpret_cast<int*>(smem);
-  int* s_hoff = s_h + x.HV;
-  const int t = threadIdx.x;
-  if (t < K) s_hoff[t] = (p.st.da[t] * x.HBB + p.st.db[t]) * x.HCC + p.st.dc[t];
-  load_halo_heights(g, p.st, x, p.h, s_h);
-  const uint64_t m = p.mask[x.gi];
-  bool boundary = false;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    int na = x.ia + p.st.da[k], nb = x.ib + p.st.db[k], nc = x.ic + p.st.dc[k];
-    if (na < 0 || na >= g.TA || nb < 0 || nb >= g.TB || nc < 0 || nc >= g.TC) boundary = true;
-  }
-  __syncthreads();
-  int my_h = s_h[x.hidx];
-  bool changed = false;
-  int converged = 0;
-  for (int it = 0; it < p.max_local; ++it) {
-    int best = my_h;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      if ((m >> k) & 1) {
-        const int hn = s_h[x.hidx + s_hoff[k]] + 1;
-        best = hn < best ? hn : best;
-      }
-    }
-    const int c = best < my_h;
-    if (c) {
-      my_h = best;
-      s_h[x.hidx] = best;
-      changed = true;
-    }
-    if (!__syncthreads_or(c)) { converged = 1; break; }
-  }
-  if (changed) p.h[x.gi] = my_h;
-  const int bch = changed && boundary;
-  const int any_b = __syncthreads_or(bch);
-  if (t == 0) {
-    if (any_b) { mark_neighbour_tiles(g, tile, p.dirty_next); *p.any_changed = 1; }
-    if (!converged) { p.dirty_next[tile] = 1; *p.any_changed = 1; }
-    p.dirty_cur[tile] = 0;
-    atomicAdd(&p.counters[1], 1ull);
-  }
-}
-
-// ----------------------------------------------------- forward closure
-
-template <int K>
-__global__ void __launch_bounds__(1024) k_reach_tile(ReachParams p) {
-  const int tile = blockIdx.x;
-  if (!p.dirty_cur[tile]) return;
-  extern __shared__ __align__(16) unsigned char smem[];
-  const Geo& g = p.g;
-  const TileCtx x = tile_ctx(g, p.st, tile);
-  int* s_mark = reinterpret_cast<int*>(smem);
-  int* s_toff = s_mark + x.NT;
-  const int t = threadIdx.x;
-  if (t < K) s_toff[t] = (p.st.da[t] * g.TB + p.st.db[t]) * g.TC + p.st.dc[t];
-  const int m0 = p.mark[x.gi];
-  s_mark[t] = m0;
-  const uint64_t m = p.mask[x.gi];
-  uint64_t outm = 0;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    int na = x.ia + p.st.da[k], nb = x.ib + p.st.db[k], nc = x.ic + p.st.dc[k];
-    if (na < 0 || na >= g.TA || nb < 0 || nb >= g.TB || nc < 0 || nc >= g.TC) outm |= 1ull << k;
-  }
-  __syncthreads();
-  int converged = 0;
-  for (int it = 0; it < p.max_local; ++it) {
-    int c = 0;
-    if (s_mark[t]) {
-      uint64_t in = m & ~outm;
-#pragma unroll
-      for (int k = 0; k < K; ++k) {
-        if ((in >> k) & 1) {
-          const int tn = t + s_toff[k];
-          if (!s_mark[tn]) { s_mark[tn] = 1; c = 1; }
-        }
-      }
-    }
-    if (!__syncthreads_or(c)) { converged = 1; break; }
-  }
-  const int mine = s_mark[t];
-  if (mine && !m0) p.mark[x.gi] = 1;
-  int sent = 0;
-  if (mine) {
-    uint64_t out = m & outm;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      if ((out >> k) & 1) {
-        const int A_ = x.a0 + x.ia + p.st.da[k], B_ = x.b0 + x.ib + p.st.db[k],
-                  C_ = x.c0 + x.ic + p.st.dc[k];
-        const long long gn = ((long long)A_ * g.Bp + B_) * g.Cp + C_;
-        if (!p.mark[gn]) {
-          p.mark[gn] = 1;
-          p.dirty_next[tile_of(g, A_, B_, C_)] = 1;
-          sent = 1;
-        }
-      }
-    }
-  }
-  const int any_sent = __syncthreads_or(sent);
-  if (t == 0) {
-    if (any_sent) *p.any_changed = 1;
-    if (!converged) { p.dirty_next[tile] = 1; *p.any_changed = 1; }
-    p.dirty_cur[tile] = 0;
-  }
-}
-
-template <typename T>
-__global__ void k_init_marks(long long n, const T* exc, int* mark) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) mark[i] = exc[i] > 0 ? 1 : 0;
-}
-
 // Bounded (row-major) outputs: cut_min from marks, cut_max from h == kHInf.
 __global__ void k_extract_cuts(Geo g, int nd, long long N, const int* mark, const int* h,
                                int* cut_min, int* cut_max) {
@@ -365,66 +176,11 @@ __global__ void k_extract_cuts(Geo g, int nd, long long N, const int* mark, cons
 
 // ------------------------------------------------------------ launchers
 
-int sm_count();
-
 size_t pr_smem_bytes_for(const Geo& g, const Stencil& st, int elem_bytes) {
-  return elem_bytes == 4 ? pr_smem_bytes<int>(g, st) : pr_smem_bytes<long long>(g, st);
+  int NT = g.TA * g.TB * g.TC;
+  int HV = (g.TA + 2 * st.HA) * (g.TB + 2 * st.HB) * (g.TC + 2 * st.HC);
+  return elem_bytes == 4 ? pool_pr_smem<int>(st.K, NT, HV) : pool_pr_smem<long long>(st.K, NT, HV);
 }
-
-cudaError_t launch_bfs_tile(const BFSParams& p, cudaStream_t s) {
-  int HV = (p.g.TA + 2 * p.st.HA) * (p.g.TB + 2 * p.st.HB) * (p.g.TC + 2 * p.st.HC);
-  size_t smem = size_t(HV + p.st.K) * sizeof(int);
-  int threads = p.g.TA * p.g.TB * p.g.TC;
-  switch (p.st.K) {
-#define X(KK)                                                   \
-  case KK:                                                      \
-    k_bfs_tile<KK><<<p.g.ntiles, threads, smem, s>>>(p); \
-    break;
-    LF_K_LIST(X)
-#undef X
-    default:
-      return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-
-cudaError_t launch_reach_tile(const ReachParams& p, cudaStream_t s) {
-  int NT = p.g.TA * p.g.TB * p.g.TC;
-  size_t smem = size_t(NT + p.st.K) * sizeof(int);
-  switch (p.st.K) {
-#define X(KK)                                                  \
-  case KK:                                                     \
-    k_reach_tile<KK><<<p.g.ntiles, NT, smem, s>>>(p); \
-    break;
-    LF_K_LIST(X)
-#undef X
-    default:
-      return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-
-template <typename T>
-cudaError_t launch_mask(const Geo& g, int K, const T* res, const uint64_t* kmask, uint64_t* mask,
-                        cudaStream_t s) {
-  int blocks = int((g.NP + 255) / 256);
-  switch (K) {
-#define X(KK)                                                      \
-  case KK:                                                         \
-    k_mask<T, KK><<<blocks, 256, 0, s>>>(g, res, kmask, mask); \
-    break;
-    LF_K_LIST(X)
-#undef X
-    default:
-      return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-
-template cudaError_t launch_mask<int>(const Geo&, int, const int*, const uint64_t*, uint64_t*,
-                                      cudaStream_t);
-template cudaError_t launch_mask<long long>(const Geo&, int, const long long*, const uint64_t*,
-                                            uint64_t*, cudaStream_t);
 
 static inline int nblk(long long n, int t) { return int((n + t - 1) / t); }
 
@@ -470,37 +226,6 @@ cudaError_t launch_sum_pos(long long n, const T* x, long long* out, cudaStream_t
 template cudaError_t launch_sum_pos<int>(long long, const int*, long long*, cudaStream_t);
 template cudaError_t launch_sum_pos<long long>(long long, const long long*, long long*,
                                                cudaStream_t);
-
-template <typename T>
-cudaError_t launch_init_heights(const Geo& g, const T* exc, const uint64_t* kmask, int* h,
-                                cudaStream_t s) {
-  k_init_heights<T><<<nblk(g.NP, 256), 256, 0, s>>>(g, exc, kmask, h);
-  return cudaGetLastError();
-}
-template cudaError_t launch_init_heights<int>(const Geo&, const int*, const uint64_t*, int*,
-                                              cudaStream_t);
-template cudaError_t launch_init_heights<long long>(const Geo&, const long long*,
-                                                    const uint64_t*, int*, cudaStream_t);
-
-template <typename T>
-cudaError_t launch_active(const Geo& g, const T* exc, const int* h, int* act,
-                          unsigned long long* count, cudaStream_t s) {
-  k_active<T><<<nblk(g.NP, 256), 256, 0, s>>>(g, exc, h, act, count);
-  return cudaGetLastError();
-}
-template cudaError_t launch_active<int>(const Geo&, const int*, const int*, int*,
-                                        unsigned long long*, cudaStream_t);
-template cudaError_t launch_active<long long>(const Geo&, const long long*, const int*, int*,
-                                              unsigned long long*, cudaStream_t);
-
-template <typename T>
-cudaError_t launch_init_marks(long long n, const T* exc, int* mark, cudaStream_t s) {
-  k_init_marks<T><<<nblk(n, 256), 256, 0, s>>>(n, exc, mark);
-  return cudaGetLastError();
-}
-template cudaError_t launch_init_marks<int>(long long, const int*, int*, cudaStream_t);
-template cudaError_t launch_init_marks<long long>(long long, const long long*, int*,
-                                                  cudaStream_t);
 
 cudaError_t launch_extract_cuts(const Geo& g, int nd, long long N, const int* mark, const int* h,
                                 int* cmin, int* cmax, cudaStream_t s) {

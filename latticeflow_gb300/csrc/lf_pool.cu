@@ -1,0 +1,591 @@
+// Host side of the instance pool and its node-level kernels.
+//
+// PoolRunner::maxflow solves every lattice of the pool to a maximum preflow:
+//   repeat {
+//     global relabel of every unfinished lattice (BFS passes draining the
+//       tile queue until no tile changes);
+//     count active nodes per lattice; a lattice with none is finished;
+//       the others get their epoch height cap (BFS depth + slack) and their
+//       active tiles queued;
+//     stop when no lattice has active nodes;
+//     `launches_per_relabel` push/relabel passes draining the tile queue
+//   }
+// Node pools hold all lattices back to back (node_base), residual planes
+// likewise (res_base); the persistent kernels take whatever tile is queued
+// next, from any lattice.
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cstring>
+
+#include "lf_pool_runner.h"
+#include "lf_pool_tile.cuh"
+
+namespace lfg {
+
+namespace {
+
+inline int nblk(long long n, int t) { return int((n + t - 1) / t); }
+
+// lattice of pool node i (node_base ascending, n entries + sentinel)
+__device__ __forceinline__ int inst_of(const long long* nbase, int n, long long i) {
+  int lo = 0, hi = n;  // nbase[lo] <= i < nbase[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (nbase[mid] <= i) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+struct NodeRef {
+  int inst;
+  long long li;
+  int a, b, c;
+};
+
+__device__ __forceinline__ NodeRef node_ref(const InstDesc* insts, const long long* nbase, int n,
+                                            long long i) {
+  NodeRef r;
+  r.inst = inst_of(nbase, n, i);
+  r.li = i - nbase[r.inst];
+  const Geo& g = insts[r.inst].g;
+  r.c = int(r.li % g.Cp);
+  r.b = int((r.li / g.Cp) % g.Bp);
+  r.a = int(r.li / ((long long)g.Cp * g.Bp));
+  return r;
+}
+
+template <typename T>
+__global__ void k_pool_init_heights(const InstDesc* insts, const long long* nbase, int n,
+                                    long long NP, const T* exc, const uint64_t* kmask, int* h) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NP) return;
+  int in = inst_of(nbase, n, i);
+  if (insts[in].done || !insts[in].active) return;
+  bool part = !kmask || (kmask[i] >> 63);
+  h[i] = (part && exc[i] < 0) ? 0 : kHInf;
+}
+
+template <typename T>
+__global__ void k_pool_mask(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                            const T* res, const uint64_t* kmask, uint64_t* mask) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NP) return;
+  int in = inst_of(nbase, n, i);
+  const InstDesc& I = insts[in];
+  if (I.done || !I.active) return;
+  long long li = i - nbase[in];
+  const T* r = res + I.res_base;
+  uint64_t m = 0;
+  for (int k = 0; k < I.st.K; ++k)
+    if (r[(long long)k * I.g.NP + li] > 0) m |= 1ull << k;
+  if (kmask) m &= kmask[i];
+  mask[i] = m;
+}
+
+// every tile of every unfinished lattice into list 0
+__global__ void k_pool_queue_all(const InstDesc* insts, const int* tile_inst, int tiles,
+                                 TileQueue q) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tiles) return;
+  const InstDesc& I = insts[tile_inst[t]];
+  if (I.done || !I.active) return;
+  enqueue_tile(q, 0, t);
+}
+
+template <typename T>
+__global__ void k_pool_active(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                              const T* exc, const int* h, TileQueue q,
+                              unsigned long long* cnt, unsigned* hmx) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NP) return;
+  NodeRef r = node_ref(insts, nbase, n, i);
+  const InstDesc& I = insts[r.inst];
+  if (I.done || !I.active) return;
+  int hh = h[i];
+  if (hh < kHInf) atomicMax(&hmx[r.inst], (unsigned)hh);
+  if (exc[i] > 0 && hh < kHInf) {
+    atomicAdd(&cnt[r.inst], 1ull);
+    enqueue_tile(q, 0, I.tile_base + tile_of(I.g, r.a, r.b, r.c));
+  }
+}
+
+// a lattice with no active node is finished; the others get their cap
+__global__ void k_pool_update(InstDesc* insts, int n, const unsigned long long* cnt,
+                              const unsigned* hmx, long long cap, int slack,
+                              unsigned long long* total) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  InstDesc& I = insts[i];
+  if (I.done || !I.active) return;
+  if (cnt[i] == 0) {
+    I.done = 1;
+    return;
+  }
+  long long hm = (long long)hmx[i] + slack;
+  long long c = cap < I.g.NP + 2 ? cap : I.g.NP + 2;
+  I.hmax = int(hm < c ? hm : c);
+  atomicAdd(total, cnt[i]);
+}
+
+__global__ void k_pool_reset(InstDesc* insts, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) insts[i].done = 0;
+}
+
+template <typename T>
+__global__ void k_pool_init_marks(const InstDesc* insts, const long long* nbase, int n,
+                                  long long NP, const T* exc, int* mark) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NP) return;
+  int in = inst_of(nbase, n, i);
+  if (!insts[in].active) return;
+  mark[i] = exc[i] > 0 ? 1 : 0;
+}
+
+__global__ void k_pool_queue_active(const InstDesc* insts, const int* tile_inst, int tiles,
+                                    TileQueue q) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tiles) return;
+  if (!insts[tile_inst[t]].active) return;
+  enqueue_tile(q, 0, t);
+}
+
+// per-lattice sum of max(exc, 0)
+template <typename T>
+__global__ void k_pool_sum_pos(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                               const T* exc, long long* sums) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NP) return;
+  int in = inst_of(nbase, n, i);
+  if (!insts[in].active) return;
+  T a = exc[i];
+  if (a > 0) atom_add(&sums[in], (long long)a);
+}
+
+template <class K>
+int occupancy_grid(K kernel, int threads, size_t smem) {
+  int dev = 0, sms = 1, per = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
+  return std::max(1, per) * sms;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- BFS
+
+__device__ __forceinline__ void bfs_tile(const PoolBFS& p, const InstDesc& I, PoolSmemHead* hd,
+                                         int* s_h, int gtile) {
+  const Geo& g = I.g;
+  const Stencil& st = I.st;
+  const int tile = gtile - I.tile_base;
+  const TileCtx x = tile_ctx(g, st, tile);
+  const int t = threadIdx.x;
+  const bool live = t < x.NT;
+  const int nxt = p.cur ^ 1;
+  int* h = p.h + I.node_base;
+  if (t < st.K) hd->hoff[t] = (st.da[t] * x.HBB + st.db[t]) * x.HCC + st.dc[t];
+  load_halo_heights(g, st, x, h, s_h);
+  uint64_t m = 0;
+  bool boundary = false;
+  if (live) {
+    m = p.mask[I.node_base + x.gi];
+    for (int k = 0; k < st.K; ++k)
+      if (outside_tile(g, x, st.da[k], st.db[k], st.dc[k])) boundary = true;
+  }
+  __syncthreads();
+  int my_h = live ? s_h[x.hidx] : kHInf;
+  bool changed = false;
+  int converged = 0;
+  for (int it = 0; it < p.max_local; ++it) {
+    int best = my_h;
+    for (uint64_t b = m; b; b &= b - 1) {
+      const int k = __ffsll((long long)b) - 1;
+      const int hn = s_h[x.hidx + hd->hoff[k]] + 1;
+      best = hn < best ? hn : best;
+    }
+    const int c = best < my_h;
+    if (c) {
+      my_h = best;
+      s_h[x.hidx] = best;
+      changed = true;
+    }
+    if (!__syncthreads_or(c)) { converged = 1; break; }
+  }
+  if (changed) h[x.gi] = my_h;
+  const int any_b = __syncthreads_or(changed && boundary);
+  if (t == 0) {
+    if (any_b) {
+      const int tc = tile % g.ntc, tb = (tile / g.ntc) % g.ntb, ta = tile / (g.ntc * g.ntb);
+      for (int da = -1; da <= 1; ++da)
+        for (int db = -1; db <= 1; ++db)
+          for (int dc = -1; dc <= 1; ++dc) {
+            int a = ta + da, b = tb + db, c = tc + dc;
+            if (a < 0 || a >= g.nta || b < 0 || b >= g.ntb || c < 0 || c >= g.ntc) continue;
+            if (da == 0 && db == 0 && dc == 0) continue;
+            enqueue_tile(p.q, nxt, I.tile_base + (a * g.ntb + b) * g.ntc + c);
+          }
+      *p.any_changed = 1;
+    }
+    if (!converged) { enqueue_tile(p.q, nxt, gtile); *p.any_changed = 1; }
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_pool_bfs(PoolBFS p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  PoolSmemHead* hd = reinterpret_cast<PoolSmemHead*>(smem);
+  int* s_h = reinterpret_cast<int*>(smem + sizeof(PoolSmemHead));
+  for (;;) {
+    const int gt = pop_tile(p.q, p.cur, &hd->slot);
+    if (gt < 0) break;
+    load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
+    if (threadIdx.x == 0) {
+      p.q.flag[p.cur][gt] = 0;
+      atomicAdd(&p.counters[1], 1ull);
+    }
+    __syncthreads();
+    if (hd->inst.done) continue;
+    bfs_tile(p, hd->inst, hd, s_h, gt);
+  }
+}
+
+// ------------------------------------------------------- forward closure
+
+__device__ __forceinline__ void reach_tile(const PoolReach& p, const InstDesc& I, PoolSmemHead* hd,
+                                           int* s_mark, int gtile) {
+  const Geo& g = I.g;
+  const Stencil& st = I.st;
+  const int tile = gtile - I.tile_base;
+  const TileCtx x = tile_ctx(g, st, tile);
+  const int t = threadIdx.x;
+  const bool live = t < x.NT;
+  const int nxt = p.cur ^ 1;
+  int* mark = p.mark + I.node_base;
+  if (t < st.K) hd->toff[t] = (st.da[t] * g.TB + st.db[t]) * g.TC + st.dc[t];
+  int m0 = 0;
+  uint64_t m = 0, outm = 0;
+  if (live) {
+    m0 = mark[x.gi];
+    s_mark[t] = m0;
+    m = p.mask[I.node_base + x.gi];
+    for (int k = 0; k < st.K; ++k)
+      if (outside_tile(g, x, st.da[k], st.db[k], st.dc[k])) outm |= 1ull << k;
+  }
+  __syncthreads();
+  int converged = 0;
+  for (int it = 0; it < p.max_local; ++it) {
+    int c = 0;
+    if (live && s_mark[t]) {
+      for (uint64_t b = m & ~outm; b; b &= b - 1) {
+        const int k = __ffsll((long long)b) - 1;
+        const int tn = t + hd->toff[k];
+        if (!s_mark[tn]) { s_mark[tn] = 1; c = 1; }
+      }
+    }
+    if (!__syncthreads_or(c)) { converged = 1; break; }
+  }
+  int sent = 0;
+  if (live && s_mark[t]) {
+    if (!m0) mark[x.gi] = 1;
+    for (uint64_t b = m & outm; b; b &= b - 1) {
+      const int k = __ffsll((long long)b) - 1;
+      const int A_ = x.a0 + x.ia + st.da[k], B_ = x.b0 + x.ib + st.db[k],
+                C_ = x.c0 + x.ic + st.dc[k];
+      const long long gn = ((long long)A_ * g.Bp + B_) * g.Cp + C_;
+      if (!mark[gn]) {
+        mark[gn] = 1;
+        enqueue_tile(p.q, nxt, I.tile_base + tile_of(g, A_, B_, C_));
+        sent = 1;
+      }
+    }
+  }
+  const int any_sent = __syncthreads_or(sent);
+  if (t == 0) {
+    if (any_sent) *p.any_changed = 1;
+    if (!converged) { enqueue_tile(p.q, nxt, gtile); *p.any_changed = 1; }
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_pool_reach(PoolReach p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  PoolSmemHead* hd = reinterpret_cast<PoolSmemHead*>(smem);
+  int* s_mark = reinterpret_cast<int*>(smem + sizeof(PoolSmemHead));
+  for (;;) {
+    const int gt = pop_tile(p.q, p.cur, &hd->slot);
+    if (gt < 0) break;
+    load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
+    if (threadIdx.x == 0) p.q.flag[p.cur][gt] = 0;
+    __syncthreads();
+    reach_tile(p, hd->inst, hd, s_mark, gt);
+  }
+}
+
+
+size_t pool_smem_head_bytes() { return sizeof(PoolSmemHead); }
+
+// ------------------------------------------------------------------ runner
+
+void PoolRunner::check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    int code = (e == cudaErrorMemoryAllocation) ? 5 : 6;
+    throw LfError{code, std::string(what) + ": " + cudaGetErrorString(e)};
+  }
+}
+
+void PoolRunner::release() {
+  cudaFree(d_inst); d_inst = nullptr;
+  cudaFree(d_nbase); d_nbase = nullptr;
+  cudaFree(d_tile_inst); d_tile_inst = nullptr;
+  for (int b = 0; b < 2; ++b) {
+    cudaFree(q.flag[b]); q.flag[b] = nullptr;
+    cudaFree(q.list[b]); q.list[b] = nullptr;
+  }
+  cudaFree(q.ctr); q.ctr = nullptr;
+  cudaFree(d_cnt); d_cnt = nullptr;
+  cudaFree(d_hmx); d_hmx = nullptr;
+  cudaFree(d_sum); d_sum = nullptr;
+  cudaFree(d_flag); d_flag = nullptr;
+  cudaFree(d_counters); d_counters = nullptr;
+  if (h_pin) { cudaFreeHost(h_pin); h_pin = nullptr; }
+}
+
+PoolRunner::~PoolRunner() { release(); }
+
+void PoolRunner::setup(const std::vector<InstDesc>& insts, cudaStream_t s) {
+  stream = s;
+  grid_bfs = grid_reach = 0;
+  host = insts;
+  n = int(insts.size());
+  tiles = 0;
+  NP = 0;
+  for (const InstDesc& I : insts) {
+    tiles += I.g.ntiles;
+    NP += I.g.NP;
+  }
+  release();
+  std::vector<long long> nb(n + 1, 0);
+  std::vector<int> ti(std::max(tiles, 1), 0);
+  for (int i = 0; i < n; ++i) {
+    nb[i] = host[i].node_base;
+    for (int t = 0; t < host[i].g.ntiles; ++t) ti[host[i].tile_base + t] = i;
+  }
+  nb[n] = NP;
+  size_t T = std::max(tiles, 1);
+  check(cudaMalloc(&d_inst, std::max(n, 1) * sizeof(InstDesc)), "cudaMalloc");
+  check(cudaMalloc(&d_nbase, (n + 1) * sizeof(long long)), "cudaMalloc");
+  check(cudaMalloc(&d_tile_inst, T * sizeof(int)), "cudaMalloc");
+  for (int b = 0; b < 2; ++b) {
+    check(cudaMalloc(&q.flag[b], T * sizeof(int)), "cudaMalloc");
+    check(cudaMalloc(&q.list[b], T * sizeof(int)), "cudaMalloc");
+    check(cudaMemsetAsync(q.flag[b], 0, T * sizeof(int), stream), "memset");
+  }
+  check(cudaMalloc(&q.ctr, 4 * sizeof(unsigned)), "cudaMalloc");
+  check(cudaMalloc(&d_cnt, std::max(n, 1) * sizeof(unsigned long long)), "cudaMalloc");
+  check(cudaMalloc(&d_hmx, std::max(n, 1) * sizeof(unsigned)), "cudaMalloc");
+  check(cudaMalloc(&d_sum, 2 * std::max(n, 1) * sizeof(long long)), "cudaMalloc");
+  check(cudaMalloc(&d_flag, sizeof(int)), "cudaMalloc");
+  check(cudaMalloc(&d_counters, 4 * sizeof(unsigned long long)), "cudaMalloc");
+  check(cudaMallocHost(&h_pin, 64), "cudaMallocHost");
+  check(cudaMemcpyAsync(d_inst, host.data(), n * sizeof(InstDesc), cudaMemcpyHostToDevice, stream), "memcpy");
+  check(cudaMemcpyAsync(d_nbase, nb.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, stream), "memcpy");
+  check(cudaMemcpyAsync(d_tile_inst, ti.data(), T * sizeof(int), cudaMemcpyHostToDevice, stream), "memcpy");
+  check(cudaMemsetAsync(d_counters, 0, 4 * sizeof(unsigned long long), stream), "memset");
+  check(cudaStreamSynchronize(stream), "sync");
+  // launch shapes: the largest tile of the pool
+  threads = 1;
+  hv_max = 0;
+  for (const InstDesc& I : host) {
+    threads = std::max(threads, I.g.TA * I.g.TB * I.g.TC);
+    hv_max = std::max(hv_max, (I.g.TA + 2 * I.st.HA) * (I.g.TB + 2 * I.st.HB) * (I.g.TC + 2 * I.st.HC));
+  }
+}
+
+void PoolRunner::prep_pass(int cur) {
+  int lo = cur ? 0 : 2;  // see TileQueue: count of the other list + this pass's head
+  check(cudaMemsetAsync(q.ctr + lo, 0, 2 * sizeof(unsigned), stream), "memset");
+}
+
+void PoolRunner::sync_read(void* dst, const void* src, size_t bytes) {
+  check(cudaMemcpyAsync(h_pin, src, bytes, cudaMemcpyDeviceToHost, stream), "memcpy");
+  check(cudaStreamSynchronize(stream), "sync");
+  std::memcpy(dst, h_pin, bytes);
+}
+
+void PoolRunner::mark(int cat, bool end) {
+  if (hooks && hooks->profiling) hooks->mark(cat, end);
+}
+
+void PoolRunner::count_launch() {
+  if (hooks) ++hooks->launches;
+}
+
+template <typename T>
+void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* mask,
+                                const uint64_t* kmask, SolveStats& stats) {
+  const int B = 256;
+  k_pool_init_heights<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, exc, kmask, h);
+  count_launch();
+  k_pool_mask<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, res, kmask, mask);
+  count_launch();
+  check(cudaMemsetAsync(q.ctr, 0, 4 * sizeof(unsigned), stream), "memset");
+  k_pool_queue_all<<<nblk(tiles, B), B, 0, stream>>>(d_inst, d_tile_inst, tiles, q);
+  count_launch();
+  check(cudaGetLastError(), "bfs setup");
+  const size_t smem = sizeof(PoolSmemHead) + size_t(hv_max) * sizeof(int);
+  if (!grid_bfs) grid_bfs = occupancy_grid(k_pool_bfs, threads, smem);
+  const int grid = grid_bfs;
+  const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
+  const long long cap = 4LL * tiles + 64;
+  int cur = 0;
+  for (long long pass = 0;;) {
+    if (pass > cap) throw LfError{4, "global relabel did not converge"};
+    for (int c = 0; c < chunk; ++c, ++pass) {
+      prep_pass(cur);
+      check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
+      PoolBFS p{d_inst, d_tile_inst, h, mask, q, cur, 64, d_flag, d_counters};
+      mark(1, false);
+      k_pool_bfs<<<grid, threads, smem, stream>>>(p);
+      check(cudaGetLastError(), "bfs pass");
+      mark(1, true);
+      count_launch();
+      ++stats.bfs_passes;
+      cur ^= 1;
+    }
+    int changed = 0;
+    sync_read(&changed, d_flag, sizeof(int));
+    if (!changed) break;
+  }
+}
+
+template <typename T>
+unsigned long long PoolRunner::activate(const T* exc, const int* h) {
+  const int B = 256;
+  check(cudaMemsetAsync(q.ctr, 0, 4 * sizeof(unsigned), stream), "memset");
+  check(cudaMemsetAsync(d_cnt, 0, n * sizeof(unsigned long long), stream), "memset");
+  check(cudaMemsetAsync(d_hmx, 0, n * sizeof(unsigned), stream), "memset");
+  check(cudaMemsetAsync(d_counters + 3, 0, sizeof(unsigned long long), stream), "memset");
+  k_pool_active<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, exc, h, q, d_cnt, d_hmx);
+  count_launch();
+  const long long hcap = (long long)kHInf - 2;
+  const int slack = tune.height_slack > 0 ? tune.height_slack : 16;
+  k_pool_update<<<nblk(n, B), B, 0, stream>>>(d_inst, n, d_cnt, d_hmx, hcap, slack, d_counters + 3);
+  count_launch();
+  check(cudaGetLastError(), "activate");
+  unsigned long long total = 0;
+  sync_read(&total, d_counters + 3, sizeof(total));
+  return total;
+}
+
+template <typename T>
+void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t* kmask, int* markv,
+                         SolveStats& stats, bool sets) {
+  const int B = 256;
+  k_pool_reset<<<nblk(n, B), B, 0, stream>>>(d_inst, n);
+  count_launch();
+  check(cudaMemsetAsync(d_counters, 0, 3 * sizeof(unsigned long long), stream), "memset");
+  const int M = tune.launches_per_relabel > 0 ? tune.launches_per_relabel : 4;
+  const int R = tune.sweeps > 0 ? tune.sweeps : 4;
+  int KA = 0, KB = 0;
+  int NTmax = 1;
+  for (const InstDesc& I : host) {
+    if (!I.active) continue;
+    if (!KA) KA = I.st.K;
+    else if (I.st.K != KA) KB = I.st.K;
+    NTmax = std::max(NTmax, I.g.TA * I.g.TB * I.g.TC);
+  }
+  if (!KB) KB = KA;
+  if (KA > KB) std::swap(KA, KB);
+  const size_t smem = pool_pr_smem<T>(KB, NTmax, hv_max);
+  const long long max_epochs = 20000;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (long long epoch = 0;; ++epoch) {
+    if (epoch > max_epochs) throw LfError{4, "push-relabel did not converge"};
+    if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(300))
+      throw LfError{4, "push-relabel exceeded its time limit"};
+    global_relabel<T>(res, exc, h, mask, kmask, stats);
+    ++stats.epochs;
+    if (activate<T>(exc, h) == 0) break;
+    int cur = 0;
+    for (int l = 0; l < M; ++l) {
+      prep_pass(cur);
+      PoolPR<T> p{d_inst, d_tile_inst, res, exc, h, kmask, q, cur, R, d_counters};
+      mark(0, false);
+      check(launch_pool_pr<T>(p, KA, KB, NTmax, smem, stream), "push-relabel pass");
+      mark(0, true);
+      count_launch();
+      ++stats.pr_launches;
+      cur ^= 1;
+    }
+    // drain what the last pass queued so the next relabel starts clean
+    check(cudaMemsetAsync(q.ctr, 0, 4 * sizeof(unsigned), stream), "memset");
+    for (int b = 0; b < 2; ++b)
+      check(cudaMemsetAsync(q.flag[b], 0, std::max(tiles, 1) * sizeof(int), stream), "memset");
+  }
+  if (sets) reach<T>(exc, mask, markv, stats);
+  unsigned long long c[2];
+  sync_read(c, d_counters, sizeof(c));
+  stats.tiles_processed = c[0];
+  stats.bfs_tiles = c[1];
+}
+
+template <typename T>
+void PoolRunner::reach(const T* exc, const uint64_t* mask, int* markv, SolveStats& stats) {
+  const int B = 256;
+  k_pool_init_marks<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, exc, markv);
+  count_launch();
+  check(cudaMemsetAsync(q.ctr, 0, 4 * sizeof(unsigned), stream), "memset");
+  k_pool_queue_active<<<nblk(tiles, B), B, 0, stream>>>(d_inst, d_tile_inst, tiles, q);
+  count_launch();
+  check(cudaGetLastError(), "reach setup");
+  int NTmax = threads;
+  const size_t smem = sizeof(PoolSmemHead) + size_t(NTmax) * sizeof(int);
+  if (!grid_reach) grid_reach = occupancy_grid(k_pool_reach, threads, smem);
+  const int grid = grid_reach;
+  const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
+  const long long cap = 4LL * tiles + 64;
+  int cur = 0;
+  for (long long pass = 0;;) {
+    if (pass > cap) throw LfError{4, "cut-set closure did not converge"};
+    for (int c = 0; c < chunk; ++c, ++pass) {
+      prep_pass(cur);
+      check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
+      PoolReach p{d_inst, d_tile_inst, markv, mask, q, cur, 256, d_flag};
+      mark(2, false);
+      k_pool_reach<<<grid, threads, smem, stream>>>(p);
+      check(cudaGetLastError(), "reach pass");
+      mark(2, true);
+      count_launch();
+      ++stats.reach_passes;
+      cur ^= 1;
+    }
+    int changed = 0;
+    sync_read(&changed, d_flag, sizeof(int));
+    if (!changed) break;
+  }
+}
+
+template <typename T>
+void PoolRunner::stuck_excess(const T* exc, long long* out_host) {
+  const int B = 256;
+  check(cudaMemsetAsync(d_sum, 0, n * sizeof(long long), stream), "memset");
+  k_pool_sum_pos<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, exc, d_sum);
+  count_launch();
+  check(cudaGetLastError(), "sum");
+  check(cudaMemcpyAsync(out_host, d_sum, n * sizeof(long long), cudaMemcpyDeviceToHost, stream), "memcpy");
+  check(cudaStreamSynchronize(stream), "sync");
+}
+
+void PoolRunner::set_active(const std::vector<int>& act) {
+  for (int i = 0; i < n; ++i) host[i].active = act[i];
+  check(cudaMemcpyAsync(d_inst, host.data(), n * sizeof(InstDesc), cudaMemcpyHostToDevice, stream), "memcpy");
+}
+
+template void PoolRunner::maxflow<int>(int*, int*, int*, uint64_t*, const uint64_t*, int*, SolveStats&, bool);
+template void PoolRunner::maxflow<long long>(long long*, long long*, int*, uint64_t*, const uint64_t*, int*, SolveStats&, bool);
+template void PoolRunner::stuck_excess<int>(const int*, long long*);
+template void PoolRunner::stuck_excess<long long>(const long long*, long long*);
+
+
+}  // namespace lfg

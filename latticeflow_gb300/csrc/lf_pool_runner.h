@@ -1,0 +1,94 @@
+// Host runner of the instance pool (see lf_pool.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "lf_pool.cuh"
+
+namespace lfg {
+
+struct LfError {
+  int code;
+  std::string msg;
+};
+
+struct Tuning {
+  int tile_rows = 0;             // TB (2-d) / TB with TA = 4 (3-d); 0 = auto
+  int sweeps = 0;                // local push/relabel rounds per tile visit
+  int launches_per_relabel = 0;  // push/relabel passes between global relabels
+  int height_slack = 0;          // heights above (BFS depth + slack) park until the next relabel
+  int pass_chunk = 0;            // BFS / closure passes launched between host checks
+};
+
+struct SolveStats {
+  long long epochs = 0, pr_launches = 0, bfs_passes = 0, reach_passes = 0;
+  unsigned long long tiles_processed = 0, bfs_tiles = 0;
+};
+
+// Profiling hooks of the owner (events around launches, launch counting).
+struct ProfHooks {
+  bool profiling = false;
+  long long launches = 0;
+  virtual void mark(int cat, bool end) = 0;
+  virtual ~ProfHooks() {}
+};
+
+size_t pool_smem_head_bytes();
+
+template <typename T>
+size_t pool_pr_smem(int K, int NT, int HV) {
+  return pool_smem_head_bytes() + size_t(K + 1) * NT * sizeof(T) + size_t(HV) * sizeof(int);
+}
+
+template <typename T>
+cudaError_t launch_pool_pr(const PoolPR<T>& p, int KA, int KB, int threads, size_t smem,
+                           cudaStream_t s);
+
+class PoolRunner {
+ public:
+  ~PoolRunner();
+  void setup(const std::vector<InstDesc>& insts, cudaStream_t s);
+  void set_active(const std::vector<int>& act);
+  template <typename T>
+  void maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t* kmask, int* mark,
+               SolveStats& stats, bool sets);
+  template <typename T> void stuck_excess(const T* exc, long long* out_host);
+
+  Tuning tune;
+  ProfHooks* hooks = nullptr;
+  std::vector<InstDesc> host;
+  int n = 0, tiles = 0;
+  long long NP = 0;
+  InstDesc* d_inst = nullptr;
+
+ private:
+  template <typename T>
+  void global_relabel(const T* res, const T* exc, int* h, uint64_t* mask, const uint64_t* kmask,
+                      SolveStats& stats);
+  template <typename T> unsigned long long activate(const T* exc, const int* h);
+  template <typename T> void reach(const T* exc, const uint64_t* mask, int* mark, SolveStats& stats);
+  void prep_pass(int cur);
+  void sync_read(void* dst, const void* src, size_t bytes);
+  void mark(int cat, bool end);
+  void count_launch();
+  void check(cudaError_t e, const char* what);
+  void release();
+
+  cudaStream_t stream = nullptr;
+  long long* d_nbase = nullptr;
+  int* d_tile_inst = nullptr;
+  TileQueue q{{nullptr, nullptr}, {nullptr, nullptr}, nullptr};
+  unsigned long long* d_cnt = nullptr;
+  unsigned* d_hmx = nullptr;
+  long long* d_sum = nullptr;
+  int* d_flag = nullptr;
+  unsigned long long* d_counters = nullptr;  // [0] pr tiles, [1] bfs tiles, [3] active total
+  void* h_pin = nullptr;
+  int threads = 1, hv_max = 0;
+  int grid_bfs = 0, grid_reach = 0;
+};
+
+}  // namespace lfg

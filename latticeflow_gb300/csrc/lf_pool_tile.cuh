@@ -1,0 +1,187 @@
+// Tile work of the pool kernels: push/relabel, BFS relabel, forward closure.
+//
+// Each persistent CTA pops one queued tile at a time, copies the tile's
+// lattice descriptor into shared memory and works on the tile:
+//
+// push/relabel (one CTA stages all residual planes, the excess and the
+// heights with a halo in shared memory, then runs up to `sweeps` rounds of)
+//   push:    every node with excess sends flow to lower neighbours with
+//            residual capacity, lowest direction index first; heights are
+//            frozen during the phase, so an edge carries flow one way only and
+//            the only shared update is the atomic excess add;
+//   relabel: a node that still has excess and no lower residual neighbour
+//            moves to one above its lowest residual neighbour, capped at the
+//            lattice's epoch limit;
+// until no node of the tile is active.  Flow pushed across the tile edge is
+// delivered with global atomics (residual of the reverse edge and the
+// neighbour's excess) and queues the neighbour tile; edge nodes write back
+// their excess as a delta for the same reason.  Stale halo heights can leave
+// labels invalid; the next global relabel recomputes them exactly, and the
+// final answer depends only on the residual graph, never on labels.
+//
+// BFS relabel: exact distance to the nearest deficit node along residual
+// edges, iterated inside the tile until stable; a changed edge node queues
+// the neighbour tiles.  Forward closure: marks spread along residual edges.
+#pragma once
+
+#include "lf_pool.cuh"
+#include "lf_tile_common.cuh"
+
+namespace lfg {
+
+struct alignas(16) PoolSmemHead {
+  InstDesc inst;
+  int slot;
+  int hoff[kMaxKDev];
+  int toff[kMaxKDev];
+};
+
+__device__ __forceinline__ void load_inst(const InstDesc* src, InstDesc* dst) {
+  const int n = int(sizeof(InstDesc) / sizeof(int));
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] = s[i];
+}
+
+__device__ __forceinline__ bool outside_tile(const Geo& g, const TileCtx& x, int da, int db,
+                                             int dc) {
+  int na = x.ia + da, nb = x.ib + db, nc = x.ic + dc;
+  return na < 0 || na >= g.TA || nb < 0 || nb >= g.TB || nc < 0 || nc >= g.TC;
+}
+
+// ------------------------------------------------------------ push/relabel
+
+template <typename T, int K>
+__device__ void pr_tile(const PoolPR<T>& p, const InstDesc& I, PoolSmemHead* hd, unsigned char* sbuf,
+                        int gtile) {
+  const Geo& g = I.g;
+  const Stencil& st = I.st;
+  const int tile = gtile - I.tile_base;
+  const TileCtx x = tile_ctx(g, st, tile);
+  const int NT = x.NT;
+  const int t = threadIdx.x;
+  const bool live = t < NT;
+  const int nxt = p.cur ^ 1;
+  T* res = p.res + I.res_base;
+  T* exc = p.exc + I.node_base;
+  int* h = p.h + I.node_base;
+  T* s_res = reinterpret_cast<T*>(sbuf);
+  T* s_exc = s_res + (size_t)K * NT;
+  int* s_h = reinterpret_cast<int*>(s_exc + NT);
+  if (t < K) {
+    hd->hoff[t] = (st.da[t] * x.HBB + st.db[t]) * x.HCC + st.dc[t];
+    hd->toff[t] = (st.da[t] * g.TB + st.db[t]) * g.TC + st.dc[t];
+  }
+  load_halo_heights(g, st, x, h, s_h);
+  uint64_t outm = 0;
+  T r0[K];
+  T e0 = 0;
+  uint64_t km = 0;
+  if (live) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      r0[k] = res[(long long)k * g.NP + x.gi];
+      s_res[k * NT + t] = r0[k];
+      if (outside_tile(g, x, st.da[k], st.db[k], st.dc[k])) outm |= 1ull << k;
+    }
+    e0 = exc[x.gi];
+    s_exc[t] = e0;
+    km = p.kmask ? p.kmask[I.node_base + x.gi] : ~0ull;
+  }
+  __syncthreads();
+  const int hmax = I.hmax;
+  int my_h = live ? s_h[x.hidx] : kHInf;
+  for (int it = 0; it < p.sweeps; ++it) {
+    T e = live ? s_exc[t] : (T)0;
+    if (e > 0 && my_h < hmax) {
+      T sent = 0;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        if (!((km >> k) & 1)) continue;
+        const T rem = e - sent;
+        if (rem <= 0) break;
+        const T r = s_res[k * NT + t];
+        if (r <= 0) continue;
+        if (s_h[x.hidx + hd->hoff[k]] >= my_h) continue;
+        const T d = rem < r ? rem : r;
+        s_res[k * NT + t] = r - d;
+        sent += d;
+        if (!((outm >> k) & 1)) {
+          const int tn = t + hd->toff[k];
+          atom_add(&s_exc[tn], d);
+          s_res[st.rev[k] * NT + tn] += d;
+        }
+      }
+      if (sent) atom_add(&s_exc[t], (T)-sent);
+    }
+    __syncthreads();
+    e = live ? s_exc[t] : (T)0;
+    int act = 0;
+    if (e > 0 && my_h < hmax) {
+      int hmin = kHInf;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        if (((km >> k) & 1) && s_res[k * NT + t] > 0) {
+          const int hn = s_h[x.hidx + hd->hoff[k]];
+          hmin = hn < hmin ? hn : hmin;
+        }
+      }
+      if (hmin >= my_h) {
+        my_h = (hmin >= hmax - 1) ? hmax : hmin + 1;
+        s_h[x.hidx] = my_h;
+      }
+      act = my_h < hmax;
+    }
+    if (!__syncthreads_or(act)) break;
+  }
+  __syncthreads();
+  int still = 0;
+  if (live) {
+    const T ef = s_exc[t];
+    if (outm) atom_add(&exc[x.gi], (T)(ef - e0));
+    else exc[x.gi] = ef;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const T rf = s_res[k * NT + t];
+      if ((outm >> k) & 1) {
+        const T d = r0[k] - rf;
+        if (d != 0) {
+          atom_add(&res[(long long)k * g.NP + x.gi], (T)-d);
+          const int A_ = x.a0 + x.ia + st.da[k], B_ = x.b0 + x.ib + st.db[k],
+                    C_ = x.c0 + x.ic + st.dc[k];
+          const long long gn = ((long long)A_ * g.Bp + B_) * g.Cp + C_;
+          atom_add(&res[(long long)st.rev[k] * g.NP + gn], d);
+          atom_add(&exc[gn], d);
+          enqueue_tile(p.q, nxt, I.tile_base + tile_of(g, A_, B_, C_));
+        }
+      } else {
+        res[(long long)k * g.NP + x.gi] = rf;
+      }
+    }
+    h[x.gi] = my_h;
+    still = ef > 0 && my_h < hmax;
+  }
+  if (__syncthreads_or(still) && t == 0) enqueue_tile(p.q, nxt, gtile);
+}
+
+template <typename T, int KA, int KB>
+__global__ void __launch_bounds__(1024) k_pool_pr(PoolPR<T> p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  PoolSmemHead* hd = reinterpret_cast<PoolSmemHead*>(smem);
+  unsigned char* sbuf = smem + sizeof(PoolSmemHead);
+  for (;;) {
+    const int gt = pop_tile(p.q, p.cur, &hd->slot);
+    if (gt < 0) break;
+    load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
+    if (threadIdx.x == 0) {
+      p.q.flag[p.cur][gt] = 0;
+      atomicAdd(&p.counters[0], 1ull);
+    }
+    __syncthreads();
+    if (hd->inst.done) continue;
+    if (hd->inst.st.K == KA) pr_tile<T, KA>(p, hd->inst, hd, sbuf, gt);
+    else if (KB != KA && hd->inst.st.K == KB) pr_tile<T, KB>(p, hd->inst, hd, sbuf, gt);
+  }
+}
+
+}  // namespace lfg

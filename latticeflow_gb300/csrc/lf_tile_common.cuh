@@ -7,7 +7,6 @@
 
 namespace lfg {
 
-#define LF_K_LIST(X) X(4) X(6) X(8) X(12) X(16) X(18) X(20) X(24) X(26) X(28) X(32) X(36) X(40) X(48)
 
 __device__ __forceinline__ int atom_add(int* p, int v) { return atomicAdd(p, v); }
 __device__ __forceinline__ long long atom_add(long long* p, long long v) {
@@ -58,25 +57,6 @@ __device__ __forceinline__ void load_halo_heights(const Geo& g, const Stencil& s
       v = h[((long long)A_ * g.Bp + B_) * g.Cp + C_];
     s_h[i] = v;
   }
-}
-
-__device__ __forceinline__ void mark_neighbour_tiles(const Geo& g, int tile, int* flags) {
-  const int tc = tile % g.ntc, tb = (tile / g.ntc) % g.ntb, ta = tile / (g.ntc * g.ntb);
-  for (int da = -1; da <= 1; ++da)
-    for (int db = -1; db <= 1; ++db)
-      for (int dc = -1; dc <= 1; ++dc) {
-        int a = ta + da, b = tb + db, c = tc + dc;
-        if (a < 0 || a >= g.nta || b < 0 || b >= g.ntb || c < 0 || c >= g.ntc) continue;
-        if (da == 0 && db == 0 && dc == 0) continue;
-        flags[(a * g.ntb + b) * g.ntc + c] = 1;
-      }
-}
-
-template <typename T>
-static inline size_t pr_smem_bytes(const Geo& g, const Stencil& st) {
-  int NT = g.TA * g.TB * g.TC;
-  int HV = (g.TA + 2 * st.HA) * (g.TB + 2 * st.HB) * (g.TC + 2 * st.HC);
-  return size_t(st.K + 1) * NT * sizeof(T) + size_t(HV + 2 * st.K) * sizeof(int);
 }
 
 }  // namespace lfg
