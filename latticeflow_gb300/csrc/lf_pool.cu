@@ -233,22 +233,24 @@ __device__ __forceinline__ void bfs_tile(const PoolBFS& p, const InstDesc& I, Po
   }
 }
 
+template <bool SINGLE>
 __global__ void __launch_bounds__(1024) k_pool_bfs(PoolBFS p) {
+  const int gt = queued_tile(p.q, p.cur);
+  if (gt < 0) return;
   extern __shared__ __align__(16) unsigned char smem[];
   PoolSmemHead* hd = reinterpret_cast<PoolSmemHead*>(smem);
   int* s_h = reinterpret_cast<int*>(smem + sizeof(PoolSmemHead));
-  for (;;) {
-    const int gt = pop_tile(p.q, p.cur, &hd->slot);
-    if (gt < 0) break;
+  if (!SINGLE) {
     load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
-    if (threadIdx.x == 0) {
-      p.q.flag[p.cur][gt] = 0;
-      atomicAdd(&p.counters[1], 1ull);
-    }
     __syncthreads();
-    if (hd->inst.done) continue;
-    bfs_tile(p, hd->inst, hd, s_h, gt);
   }
+  const InstDesc& I = SINGLE ? p.inst0 : hd->inst;
+  if (threadIdx.x == 0) {
+    p.q.flag[p.cur][gt] = 0;
+    atomicAdd(&p.counters[1], 1ull);
+  }
+  if (I.done) return;
+  bfs_tile(p, I, hd, s_h, gt);
 }
 
 // ------------------------------------------------------- forward closure
@@ -308,18 +310,20 @@ __device__ __forceinline__ void reach_tile(const PoolReach& p, const InstDesc& I
   }
 }
 
+template <bool SINGLE>
 __global__ void __launch_bounds__(1024) k_pool_reach(PoolReach p) {
+  const int gt = queued_tile(p.q, p.cur);
+  if (gt < 0) return;
   extern __shared__ __align__(16) unsigned char smem[];
   PoolSmemHead* hd = reinterpret_cast<PoolSmemHead*>(smem);
   int* s_mark = reinterpret_cast<int*>(smem + sizeof(PoolSmemHead));
-  for (;;) {
-    const int gt = pop_tile(p.q, p.cur, &hd->slot);
-    if (gt < 0) break;
+  if (!SINGLE) {
     load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
-    if (threadIdx.x == 0) p.q.flag[p.cur][gt] = 0;
     __syncthreads();
-    reach_tile(p, hd->inst, hd, s_mark, gt);
   }
+  const InstDesc& I = SINGLE ? p.inst0 : hd->inst;
+  if (threadIdx.x == 0) p.q.flag[p.cur][gt] = 0;
+  reach_tile(p, I, hd, s_mark, gt);
 }
 
 
@@ -387,7 +391,7 @@ void PoolRunner::setup(const std::vector<InstDesc>& insts, cudaStream_t s) {
   check(cudaMalloc(&d_sum, 2 * std::max(n, 1) * sizeof(long long)), "cudaMalloc");
   check(cudaMalloc(&d_flag, sizeof(int)), "cudaMalloc");
   check(cudaMalloc(&d_counters, 4 * sizeof(unsigned long long)), "cudaMalloc");
-  check(cudaMallocHost(&h_pin, 64), "cudaMallocHost");
+  check(cudaMallocHost(&h_pin, 4096), "cudaMallocHost");
   check(cudaMemcpyAsync(d_inst, host.data(), n * sizeof(InstDesc), cudaMemcpyHostToDevice, stream), "memcpy");
   check(cudaMemcpyAsync(d_nbase, nb.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, stream), "memcpy");
   check(cudaMemcpyAsync(d_tile_inst, ti.data(), T * sizeof(int), cudaMemcpyHostToDevice, stream), "memcpy");
@@ -434,8 +438,7 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
   count_launch();
   check(cudaGetLastError(), "bfs setup");
   const size_t smem = sizeof(PoolSmemHead) + size_t(hv_max) * sizeof(int);
-  if (!grid_bfs) grid_bfs = occupancy_grid(k_pool_bfs, threads, smem);
-  const int grid = grid_bfs;
+  const int grid = std::max(tiles, 1);
   const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
   const long long cap = 4LL * tiles + 64;
   int cur = 0;
@@ -444,9 +447,10 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
     for (int c = 0; c < chunk; ++c, ++pass) {
       prep_pass(cur);
       check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
-      PoolBFS p{d_inst, d_tile_inst, h, mask, q, cur, 64, d_flag, d_counters};
+      PoolBFS p{host[0], d_inst, d_tile_inst, h, mask, q, cur, 64, d_flag, d_counters};
       mark(1, false);
-      k_pool_bfs<<<grid, threads, smem, stream>>>(p);
+      if (n == 1) k_pool_bfs<true><<<grid, threads, smem, stream>>>(p);
+      else k_pool_bfs<false><<<grid, threads, smem, stream>>>(p);
       check(cudaGetLastError(), "bfs pass");
       mark(1, true);
       count_launch();
@@ -475,6 +479,8 @@ unsigned long long PoolRunner::activate(const T* exc, const int* h) {
   check(cudaGetLastError(), "activate");
   unsigned long long total = 0;
   sync_read(&total, d_counters + 3, sizeof(total));
+  // a pool of one passes its descriptor by value: refresh cap / finished flag
+  if (n == 1) sync_read(&host[0], d_inst, sizeof(InstDesc));
   return total;
 }
 
@@ -484,6 +490,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   const int B = 256;
   k_pool_reset<<<nblk(n, B), B, 0, stream>>>(d_inst, n);
   count_launch();
+  for (InstDesc& I : host) I.done = 0;
   check(cudaMemsetAsync(d_counters, 0, 3 * sizeof(unsigned long long), stream), "memset");
   const int M = tune.launches_per_relabel > 0 ? tune.launches_per_relabel : 4;
   const int R = tune.sweeps > 0 ? tune.sweeps : 4;
@@ -510,9 +517,10 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
     int cur = 0;
     for (int l = 0; l < M; ++l) {
       prep_pass(cur);
-      PoolPR<T> p{d_inst, d_tile_inst, res, exc, h, kmask, q, cur, R, d_counters};
+      PoolPR<T> p{host[0], d_inst, d_tile_inst, res, exc, h, kmask, q, cur, R, d_counters};
       mark(0, false);
-      check(launch_pool_pr<T>(p, KA, KB, NTmax, smem, stream), "push-relabel pass");
+      check(launch_pool_pr<T>(p, KA, KB, NTmax, smem, n == 1, std::max(tiles, 1), stream),
+            "push-relabel pass");
       mark(0, true);
       count_launch();
       ++stats.pr_launches;
@@ -541,8 +549,7 @@ void PoolRunner::reach(const T* exc, const uint64_t* mask, int* markv, SolveStat
   check(cudaGetLastError(), "reach setup");
   int NTmax = threads;
   const size_t smem = sizeof(PoolSmemHead) + size_t(NTmax) * sizeof(int);
-  if (!grid_reach) grid_reach = occupancy_grid(k_pool_reach, threads, smem);
-  const int grid = grid_reach;
+  const int grid = std::max(tiles, 1);
   const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
   const long long cap = 4LL * tiles + 64;
   int cur = 0;
@@ -551,9 +558,10 @@ void PoolRunner::reach(const T* exc, const uint64_t* mask, int* markv, SolveStat
     for (int c = 0; c < chunk; ++c, ++pass) {
       prep_pass(cur);
       check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
-      PoolReach p{d_inst, d_tile_inst, markv, mask, q, cur, 256, d_flag};
+      PoolReach p{host[0], d_inst, d_tile_inst, markv, mask, q, cur, 256, d_flag};
       mark(2, false);
-      k_pool_reach<<<grid, threads, smem, stream>>>(p);
+      if (n == 1) k_pool_reach<true><<<grid, threads, smem, stream>>>(p);
+      else k_pool_reach<false><<<grid, threads, smem, stream>>>(p);
       check(cudaGetLastError(), "reach pass");
       mark(2, true);
       count_launch();

@@ -41,6 +41,7 @@ struct TileQueue {
 
 template <typename T>
 struct PoolPR {
+  InstDesc inst0;         // the lattice itself when the pool holds one
   InstDesc* inst;
   const int* tile_inst;
   T* res;
@@ -54,6 +55,7 @@ struct PoolPR {
 };
 
 struct PoolBFS {
+  InstDesc inst0;
   InstDesc* inst;
   const int* tile_inst;
   int* h;
@@ -66,6 +68,7 @@ struct PoolBFS {
 };
 
 struct PoolReach {
+  InstDesc inst0;
   InstDesc* inst;
   const int* tile_inst;
   int* mark;
@@ -84,16 +87,11 @@ __device__ __forceinline__ void enqueue_tile(const TileQueue& q, int nxt, int t)
   }
 }
 
-// Block-uniform pop of the next queued tile; -1 when the pass is drained.
-__device__ __forceinline__ int pop_tile(const TileQueue& q, int cur, int* s_slot) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned i = atomicAdd(&q.ctr[q_head_idx(cur)], 1u);
-    unsigned n = *((volatile unsigned*)&q.ctr[q_count_idx(cur)]);
-    *s_slot = i < n ? q.list[cur][i] : -1;
-  }
-  __syncthreads();
-  return *s_slot;
+// Block b of a pass works on entry b of the queue; blocks past the number of
+// queued tiles return at once (the grid covers every tile of the pool).
+__device__ __forceinline__ int queued_tile(const TileQueue& q, int cur) {
+  const unsigned n = *((volatile unsigned*)&q.ctr[q_count_idx(cur)]);
+  return blockIdx.x < n ? q.list[cur][blockIdx.x] : -1;
 }
 #endif  // __CUDACC__
 

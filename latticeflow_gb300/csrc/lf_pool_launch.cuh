@@ -15,27 +15,24 @@ namespace lfg {
 
 template <typename T>
 cudaError_t launch_pool_pr(const PoolPR<T>& p, int KA, int KB, int threads, size_t smem,
-                           cudaStream_t s) {
-  int dev = 0, sms = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-#define X(A, B)                                                                           \
-  if (KA == A && KB == B) {                                                               \
-    static int grid = 0, grid_threads = 0;                                                \
-    static size_t grid_smem = 0;                                                          \
-    if (!grid || grid_smem != smem || grid_threads != threads) {                          \
-      cudaFuncSetAttribute(k_pool_pr<T, A, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                           227 * 1024);                                                   \
-      cudaFuncSetAttribute(k_pool_pr<T, A, B>,                                            \
-                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);          \
-      int per = 1;                                                                        \
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pool_pr<T, A, B>, threads, smem); \
-      grid = (per > 0 ? per : 1) * sms;                                                   \
-      grid_smem = smem;                                                                   \
-      grid_threads = threads;                                                             \
-    }                                                                                     \
-    k_pool_pr<T, A, B><<<grid, threads, smem, s>>>(p);                                    \
-    return cudaGetLastError();                                                            \
+                           bool single, int grid, cudaStream_t s) {
+#define X(A, B)                                                                            \
+  if (KA == A && KB == B) {                                                                \
+    static bool attr = false;                                                              \
+    if (!attr) {                                                                           \
+      cudaFuncSetAttribute(k_pool_pr<T, A, B, true>,                                       \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);       \
+      cudaFuncSetAttribute(k_pool_pr<T, A, B, false>,                                      \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);       \
+      cudaFuncSetAttribute(k_pool_pr<T, A, B, true>,                                       \
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);           \
+      cudaFuncSetAttribute(k_pool_pr<T, A, B, false>,                                      \
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);           \
+      attr = true;                                                                         \
+    }                                                                                      \
+    if (single) k_pool_pr<T, A, B, true><<<grid, threads, smem, s>>>(p);                   \
+    else k_pool_pr<T, A, B, false><<<grid, threads, smem, s>>>(p);                         \
+    return cudaGetLastError();                                                             \
   }
   LF_POOL_PR_LIST(X)
 #undef X

@@ -45,7 +45,7 @@ size_t pool_pr_smem(int K, int NT, int HV) {
 
 template <typename T>
 cudaError_t launch_pool_pr(const PoolPR<T>& p, int KA, int KB, int threads, size_t smem,
-                           cudaStream_t s);
+                           bool single, int grid, cudaStream_t s);
 
 class PoolRunner {
  public:
