@@ -216,19 +216,16 @@ __device__ __forceinline__ void bfs_tile(const PoolBFS& p, const InstDesc& I, Po
   }
   if (changed) h[x.gi] = my_h;
   const int any_b = __syncthreads_or(changed && boundary);
+  // neighbour tiles are queued by 26 threads at once (one atomic pair each)
+  if (any_b && t < 27 && t != 13) {
+    const int da = t / 9 - 1, db = (t / 3) % 3 - 1, dc = t % 3 - 1;
+    const int tc = tile % g.ntc, tb = (tile / g.ntc) % g.ntb, ta = tile / (g.ntc * g.ntb);
+    const int a = ta + da, b = tb + db, c = tc + dc;
+    if (a >= 0 && a < g.nta && b >= 0 && b < g.ntb && c >= 0 && c < g.ntc)
+      enqueue_tile(p.q, nxt, I.tile_base + (a * g.ntb + b) * g.ntc + c);
+  }
   if (t == 0) {
-    if (any_b) {
-      const int tc = tile % g.ntc, tb = (tile / g.ntc) % g.ntb, ta = tile / (g.ntc * g.ntb);
-      for (int da = -1; da <= 1; ++da)
-        for (int db = -1; db <= 1; ++db)
-          for (int dc = -1; dc <= 1; ++dc) {
-            int a = ta + da, b = tb + db, c = tc + dc;
-            if (a < 0 || a >= g.nta || b < 0 || b >= g.ntb || c < 0 || c >= g.ntc) continue;
-            if (da == 0 && db == 0 && dc == 0) continue;
-            enqueue_tile(p.q, nxt, I.tile_base + (a * g.ntb + b) * g.ntc + c);
-          }
-      *p.any_changed = 1;
-    }
+    if (any_b) *p.any_changed = 1;
     if (!converged) { enqueue_tile(p.q, nxt, gtile); *p.any_changed = 1; }
   }
 }
