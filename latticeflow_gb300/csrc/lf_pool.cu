@@ -93,20 +93,34 @@ __global__ void k_pool_queue_all(const InstDesc* insts, const int* tile_inst, in
   enqueue_tile(q, 0, t);
 }
 
+// Lanes of a warp that belong to the same lattice combine their count and
+// maximum height first, so each warp issues one atomic per lattice it spans.
 template <typename T>
 __global__ void k_pool_active(const InstDesc* insts, const long long* nbase, int n, long long NP,
                               const T* exc, const int* h, TileQueue q,
                               unsigned long long* cnt, unsigned* hmx) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= NP) return;
-  NodeRef r = node_ref(insts, nbase, n, i);
-  const InstDesc& I = insts[r.inst];
-  if (I.done || !I.active) return;
-  int hh = h[i];
-  if (hh < kHInf) atomicMax(&hmx[r.inst], (unsigned)hh);
-  if (exc[i] > 0 && hh < kHInf) {
-    atomicAdd(&cnt[r.inst], 1ull);
-    enqueue_tile(q, 0, I.tile_base + tile_of(I.g, r.a, r.b, r.c));
+  int inst = -1;
+  unsigned hv = 0, act = 0;
+  if (i < NP) {
+    NodeRef r = node_ref(insts, nbase, n, i);
+    const InstDesc& I = insts[r.inst];
+    if (!I.done && I.active) {
+      inst = r.inst;
+      int hh = h[i];
+      if (hh < kHInf) hv = (unsigned)hh;
+      if (exc[i] > 0 && hh < kHInf) {
+        act = 1;
+        enqueue_tile(q, 0, I.tile_base + tile_of(I.g, r.a, r.b, r.c));
+      }
+    }
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, inst);
+  const unsigned hm = __reduce_max_sync(peers, hv);
+  const unsigned na = __reduce_add_sync(peers, act);
+  if (inst >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) {
+    if (hm) atomicMax(&hmx[inst], hm);
+    if (na) atomicAdd(&cnt[inst], (unsigned long long)na);
   }
 }
 
@@ -151,16 +165,25 @@ __global__ void k_pool_queue_active(const InstDesc* insts, const int* tile_inst,
   enqueue_tile(q, 0, t);
 }
 
-// per-lattice sum of max(exc, 0)
+// per-lattice sum of max(exc, 0), combined per warp and lattice first
 template <typename T>
 __global__ void k_pool_sum_pos(const InstDesc* insts, const long long* nbase, int n, long long NP,
                                const T* exc, long long* sums) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= NP) return;
-  int in = inst_of(nbase, n, i);
-  if (!insts[in].active) return;
-  T a = exc[i];
-  if (a > 0) atom_add(&sums[in], (long long)a);
+  int inst = -1;
+  long long v = 0;
+  if (i < NP) {
+    int in = inst_of(nbase, n, i);
+    if (insts[in].active) {
+      inst = in;
+      T a = exc[i];
+      v = a > 0 ? (long long)a : 0;
+    }
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, inst);
+  long long sum = 0;
+  for (unsigned m = peers; m; m &= m - 1) sum += __shfl_sync(peers, v, __ffs(m) - 1);
+  if (inst >= 0 && sum && (threadIdx.x & 31) == __ffs(peers) - 1) atom_add(&sums[inst], sum);
 }
 
 template <class K>
