@@ -254,7 +254,7 @@ __device__ __forceinline__ void bfs_tile(const PoolBFS& p, const InstDesc& I, Po
 }
 
 template <bool SINGLE>
-__global__ void __launch_bounds__(1024) k_pool_bfs(PoolBFS p) {
+__global__ void __launch_bounds__(1024, 2) k_pool_bfs(PoolBFS p) {
   const int gt = queued_tile(p.q, p.cur);
   if (gt < 0) return;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -331,7 +331,7 @@ __device__ __forceinline__ void reach_tile(const PoolReach& p, const InstDesc& I
 }
 
 template <bool SINGLE>
-__global__ void __launch_bounds__(1024) k_pool_reach(PoolReach p) {
+__global__ void __launch_bounds__(1024, 2) k_pool_reach(PoolReach p) {
   const int gt = queued_tile(p.q, p.cur);
   if (gt < 0) return;
   extern __shared__ __align__(16) unsigned char smem[];
