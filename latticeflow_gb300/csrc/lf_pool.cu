@@ -197,156 +197,6 @@ int occupancy_grid(K kernel, int threads, size_t smem) {
 
 }  // namespace
 
-// ---------------------------------------------------------------- BFS
-
-__device__ __forceinline__ void bfs_tile(const PoolBFS& p, const InstDesc& I, PoolSmemHead* hd,
-                                         int* s_h, int gtile) {
-  const Geo& g = I.g;
-  const Stencil& st = I.st;
-  const int tile = gtile - I.tile_base;
-  const TileCtx x = tile_ctx(g, st, tile);
-  const int t = threadIdx.x;
-  const bool live = t < x.NT;
-  const int nxt = p.cur ^ 1;
-  int* h = p.h + I.node_base;
-  if (t < st.K) hd->hoff[t] = (st.da[t] * x.HBB + st.db[t]) * x.HCC + st.dc[t];
-  load_halo_heights(g, st, x, h, s_h);
-  uint64_t m = 0;
-  bool boundary = false;
-  if (live) {
-    m = p.mask[I.node_base + x.gi];
-    for (int k = 0; k < st.K; ++k)
-      if (outside_tile(g, x, st.da[k], st.db[k], st.dc[k])) boundary = true;
-  }
-  __syncthreads();
-  int my_h = live ? s_h[x.hidx] : kHInf;
-  bool changed = false;
-  int converged = 0;
-  for (int it = 0; it < p.max_local; ++it) {
-    int best = my_h;
-    for (uint64_t b = m; b; b &= b - 1) {
-      const int k = __ffsll((long long)b) - 1;
-      const int hn = s_h[x.hidx + hd->hoff[k]] + 1;
-      best = hn < best ? hn : best;
-    }
-    const int c = best < my_h;
-    if (c) {
-      my_h = best;
-      s_h[x.hidx] = best;
-      changed = true;
-    }
-    if (!__syncthreads_or(c)) { converged = 1; break; }
-  }
-  if (changed) h[x.gi] = my_h;
-  const int any_b = __syncthreads_or(changed && boundary);
-  // neighbour tiles are queued by 26 threads at once (one atomic pair each)
-  if (any_b && t < 27 && t != 13) {
-    const int da = t / 9 - 1, db = (t / 3) % 3 - 1, dc = t % 3 - 1;
-    const int tc = tile % g.ntc, tb = (tile / g.ntc) % g.ntb, ta = tile / (g.ntc * g.ntb);
-    const int a = ta + da, b = tb + db, c = tc + dc;
-    if (a >= 0 && a < g.nta && b >= 0 && b < g.ntb && c >= 0 && c < g.ntc)
-      enqueue_tile(p.q, nxt, I.tile_base + (a * g.ntb + b) * g.ntc + c);
-  }
-  if (t == 0) {
-    if (any_b) *p.any_changed = 1;
-    if (!converged) { enqueue_tile(p.q, nxt, gtile); *p.any_changed = 1; }
-  }
-}
-
-template <bool SINGLE>
-__global__ void __launch_bounds__(1024, 2) k_pool_bfs(PoolBFS p) {
-  const int gt = queued_tile(p.q, p.cur);
-  if (gt < 0) return;
-  extern __shared__ __align__(16) unsigned char smem[];
-  PoolSmemHead* hd = reinterpret_cast<PoolSmemHead*>(smem);
-  int* s_h = reinterpret_cast<int*>(smem + sizeof(PoolSmemHead));
-  if (!SINGLE) {
-    load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
-    __syncthreads();
-  }
-  const InstDesc& I = SINGLE ? p.inst0 : hd->inst;
-  if (threadIdx.x == 0) {
-    p.q.flag[p.cur][gt] = 0;
-    atomicAdd(&p.counters[1], 1ull);
-  }
-  if (I.done) return;
-  bfs_tile(p, I, hd, s_h, gt);
-}
-
-// ------------------------------------------------------- forward closure
-
-__device__ __forceinline__ void reach_tile(const PoolReach& p, const InstDesc& I, PoolSmemHead* hd,
-                                           int* s_mark, int gtile) {
-  const Geo& g = I.g;
-  const Stencil& st = I.st;
-  const int tile = gtile - I.tile_base;
-  const TileCtx x = tile_ctx(g, st, tile);
-  const int t = threadIdx.x;
-  const bool live = t < x.NT;
-  const int nxt = p.cur ^ 1;
-  int* mark = p.mark + I.node_base;
-  if (t < st.K) hd->toff[t] = (st.da[t] * g.TB + st.db[t]) * g.TC + st.dc[t];
-  int m0 = 0;
-  uint64_t m = 0, outm = 0;
-  if (live) {
-    m0 = mark[x.gi];
-    s_mark[t] = m0;
-    m = p.mask[I.node_base + x.gi];
-    for (int k = 0; k < st.K; ++k)
-      if (outside_tile(g, x, st.da[k], st.db[k], st.dc[k])) outm |= 1ull << k;
-  }
-  __syncthreads();
-  int converged = 0;
-  for (int it = 0; it < p.max_local; ++it) {
-    int c = 0;
-    if (live && s_mark[t]) {
-      for (uint64_t b = m & ~outm; b; b &= b - 1) {
-        const int k = __ffsll((long long)b) - 1;
-        const int tn = t + hd->toff[k];
-        if (!s_mark[tn]) { s_mark[tn] = 1; c = 1; }
-      }
-    }
-    if (!__syncthreads_or(c)) { converged = 1; break; }
-  }
-  int sent = 0;
-  if (live && s_mark[t]) {
-    if (!m0) mark[x.gi] = 1;
-    for (uint64_t b = m & outm; b; b &= b - 1) {
-      const int k = __ffsll((long long)b) - 1;
-      const int A_ = x.a0 + x.ia + st.da[k], B_ = x.b0 + x.ib + st.db[k],
-                C_ = x.c0 + x.ic + st.dc[k];
-      const long long gn = ((long long)A_ * g.Bp + B_) * g.Cp + C_;
-      if (!mark[gn]) {
-        mark[gn] = 1;
-        enqueue_tile(p.q, nxt, I.tile_base + tile_of(g, A_, B_, C_));
-        sent = 1;
-      }
-    }
-  }
-  const int any_sent = __syncthreads_or(sent);
-  if (t == 0) {
-    if (any_sent) *p.any_changed = 1;
-    if (!converged) { enqueue_tile(p.q, nxt, gtile); *p.any_changed = 1; }
-  }
-}
-
-template <bool SINGLE>
-__global__ void __launch_bounds__(1024, 2) k_pool_reach(PoolReach p) {
-  const int gt = queued_tile(p.q, p.cur);
-  if (gt < 0) return;
-  extern __shared__ __align__(16) unsigned char smem[];
-  PoolSmemHead* hd = reinterpret_cast<PoolSmemHead*>(smem);
-  int* s_mark = reinterpret_cast<int*>(smem + sizeof(PoolSmemHead));
-  if (!SINGLE) {
-    load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
-    __syncthreads();
-  }
-  const InstDesc& I = SINGLE ? p.inst0 : hd->inst;
-  if (threadIdx.x == 0) p.q.flag[p.cur][gt] = 0;
-  reach_tile(p, I, hd, s_mark, gt);
-}
-
-
 size_t pool_smem_head_bytes() { return sizeof(PoolSmemHead); }
 
 // ------------------------------------------------------------------ runner
@@ -417,7 +267,15 @@ void PoolRunner::setup(const std::vector<InstDesc>& insts, cudaStream_t s) {
   check(cudaMemcpyAsync(d_tile_inst, ti.data(), T * sizeof(int), cudaMemcpyHostToDevice, stream), "memcpy");
   check(cudaMemsetAsync(d_counters, 0, 4 * sizeof(unsigned long long), stream), "memset");
   check(cudaStreamSynchronize(stream), "sync");
-  // launch shapes: the largest tile of the pool
+  // kernel sizes of the pool (at most two distinct) and launch shapes
+  ka = kb = 0;
+  for (const InstDesc& I : host) {
+    if (!ka) ka = I.st.K;
+    else if (I.st.K != ka && !kb) kb = I.st.K;
+    else if (I.st.K != ka && I.st.K != kb) throw LfError{2, "a pool mixes at most two kernel sizes"};
+  }
+  if (!kb) kb = ka;
+  if (ka > kb) std::swap(ka, kb);
   threads = 1;
   hv_max = 0;
   for (const InstDesc& I : host) {
@@ -469,8 +327,7 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
       check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
       PoolBFS p{host[0], d_inst, d_tile_inst, h, mask, q, cur, 64, d_flag, d_counters};
       mark(1, false);
-      if (n == 1) k_pool_bfs<true><<<grid, threads, smem, stream>>>(p);
-      else k_pool_bfs<false><<<grid, threads, smem, stream>>>(p);
+      check(launch_pool_bfs(p, ka, kb, n == 1, grid, threads, smem, stream), "bfs pass");
       check(cudaGetLastError(), "bfs pass");
       mark(1, true);
       count_launch();
@@ -514,16 +371,8 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   check(cudaMemsetAsync(d_counters, 0, 3 * sizeof(unsigned long long), stream), "memset");
   const int M = tune.launches_per_relabel > 0 ? tune.launches_per_relabel : 4;
   const int R = tune.sweeps > 0 ? tune.sweeps : 4;
-  int KA = 0, KB = 0;
-  int NTmax = 1;
-  for (const InstDesc& I : host) {
-    if (!I.active) continue;
-    if (!KA) KA = I.st.K;
-    else if (I.st.K != KA) KB = I.st.K;
-    NTmax = std::max(NTmax, I.g.TA * I.g.TB * I.g.TC);
-  }
-  if (!KB) KB = KA;
-  if (KA > KB) std::swap(KA, KB);
+  const int KA = ka, KB = kb;
+  const int NTmax = threads;
   const size_t smem = pool_pr_smem<T>(KB, NTmax, hv_max);
   const long long max_epochs = 20000;
   const auto t0 = std::chrono::steady_clock::now();
@@ -580,8 +429,7 @@ void PoolRunner::reach(const T* exc, const uint64_t* mask, int* markv, SolveStat
       check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
       PoolReach p{host[0], d_inst, d_tile_inst, markv, mask, q, cur, 256, d_flag};
       mark(2, false);
-      if (n == 1) k_pool_reach<true><<<grid, threads, smem, stream>>>(p);
-      else k_pool_reach<false><<<grid, threads, smem, stream>>>(p);
+      check(launch_pool_reach(p, ka, kb, n == 1, grid, threads, smem, stream), "reach pass");
       check(cudaGetLastError(), "reach pass");
       mark(2, true);
       count_launch();

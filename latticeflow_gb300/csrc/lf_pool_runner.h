@@ -47,6 +47,11 @@ template <typename T>
 cudaError_t launch_pool_pr(const PoolPR<T>& p, int KA, int KB, int threads, size_t smem,
                            bool single, int grid, cudaStream_t s);
 
+cudaError_t launch_pool_bfs(const PoolBFS& p, int KA, int KB, bool single, int grid, int threads,
+                            size_t smem, cudaStream_t s);
+cudaError_t launch_pool_reach(const PoolReach& p, int KA, int KB, bool single, int grid,
+                              int threads, size_t smem, cudaStream_t s);
+
 class PoolRunner {
  public:
   ~PoolRunner();
@@ -88,6 +93,7 @@ class PoolRunner {
   unsigned long long* d_counters = nullptr;  // [0] pr tiles, [1] bfs tiles, [3] active total
   void* h_pin = nullptr;
   int threads = 1, hv_max = 0;
+  int ka = 0, kb = 0;  // kernel sizes present in the pool
   int grid_bfs = 0, grid_reach = 0;
 };
 
