@@ -152,6 +152,33 @@ int lf_set_tuning(lf_lattice* h, int tile_rows, int local_sweeps, int launches_p
  * "height_slack", "pass_chunk".  LF_ERR_INVALID for an unknown name. */
 int lf_set_param(lf_lattice* h, const char* name, int value);
 
+/* -------------------------------------------------------------- batches
+ * Many independent lattices of uneven shapes solved together: one instance
+ * pool, every pass of the solve one launch over the queued tiles of ALL
+ * lattices.  No reference counterpart (the reference solves one lattice per
+ * interface object); each lattice's results equal a plain solve of it.
+ * Lattices are added before the first fill; a batch mixes at most two kernel
+ * sizes (Full2d_4 with Full2d_8).  Fill and result calls take the lattice
+ * index returned by lf_batch_add. */
+typedef struct lf_batch lf_batch;
+int lf_batch_create(lf_batch** out);
+void lf_batch_destroy(lf_batch* b);
+int lf_batch_add(lf_batch* b, const char* kernel, int nd, const size_t* dims, int* index_out);
+int lf_batch_size(const lf_batch* b);
+int lf_batch_add_energy_potentials(lf_batch* b, int index, const int64_t* unary,
+                                   const int64_t* binary);
+int lf_batch_add_capacities(lf_batch* b, int index, const int32_t* source, const int32_t* sink,
+                            const int32_t* edge);
+int lf_batch_clear(lf_batch* b);
+int lf_batch_run(lf_batch* b);
+double lf_batch_run_time(const lf_batch* b);
+int lf_batch_get_cut(lf_batch* b, int index, int* cut_out);
+int lf_batch_get_cut_max(lf_batch* b, int index, int* cut_out);
+int lf_batch_get_flow(lf_batch* b, int index, int64_t* flow, int64_t* energy);
+int lf_batch_set_param(lf_batch* b, const char* name, int value);
+/* epochs, push/relabel passes, BFS passes of the last run */
+int lf_batch_get_stats(const lf_batch* b, int64_t* epochs, int64_t* pr_passes, int64_t* bfs_passes);
+
 /* ------------------------------------------------------------------- TV
  * calculate2dTV<Kernel, int64>(nx, ny, f, lambda) (tv/tv_solver.hpp:650-655):
  * the single-lambda TV solve on the GPU.  f, out: nx*ny doubles, row-major.

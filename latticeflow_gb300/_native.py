@@ -46,6 +46,20 @@ PROTOTYPES = {
     "lf_get_stream": (I, [P, P]),
     "lf_get_layout": (I, [P, P, P, P]),
     "lf_tv_2d": (I, [ctypes.c_char_p, SZ, SZ, P, ctypes.c_double, P, P]),
+    "lf_batch_create": (I, [P]),
+    "lf_batch_destroy": (None, [P]),
+    "lf_batch_add": (I, [P, ctypes.c_char_p, I, P, P]),
+    "lf_batch_size": (I, [P]),
+    "lf_batch_add_energy_potentials": (I, [P, I, P, P]),
+    "lf_batch_add_capacities": (I, [P, I, P, P, P]),
+    "lf_batch_clear": (I, [P]),
+    "lf_batch_run": (I, [P]),
+    "lf_batch_run_time": (ctypes.c_double, [P]),
+    "lf_batch_get_cut": (I, [P, I, P]),
+    "lf_batch_get_cut_max": (I, [P, I, P]),
+    "lf_batch_get_flow": (I, [P, I, P, P]),
+    "lf_batch_set_param": (I, [P, ctypes.c_char_p, I]),
+    "lf_batch_get_stats": (I, [P, P, P, P]),
 }
 
 LF_OK = 0

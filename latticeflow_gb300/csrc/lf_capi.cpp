@@ -5,10 +5,14 @@
 #include <string>
 
 #include "../../include/latticeflow_gpu.h"
-#include "lf_engine.h"
+#include "lf_batch.h"
 
 struct lf_lattice {
   lfg::Engine* e;
+};
+
+struct lf_batch {
+  lfg::Batch* b;
 };
 
 namespace lfg {
@@ -282,6 +286,121 @@ int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double l
     int rc = lfg::tv_2d(k, nx, ny, f, lambda, out, levels_out);
     if (rc) throw lfg::LfError{rc, "tv solve failed"};
   });
+}
+
+// ----------------------------------------------------------------- batches
+
+int lf_batch_create(lf_batch** out) {
+  return guarded([&] {
+    if (!out) throw lfg::LfError{LF_ERR_INVALID, "null output handle"};
+    *out = nullptr;
+    lf_batch* h = new lf_batch;
+    try {
+      h->b = new lfg::Batch();
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+void lf_batch_destroy(lf_batch* b) {
+  if (!b) return;
+  delete b->b;
+  delete b;
+}
+
+int lf_batch_add(lf_batch* b, const char* kernel, int nd, const size_t* dims, int* index_out) {
+  return guarded([&] {
+    if (!b || !dims) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    const lfg::KernelDef* k = kernel ? lfg::find_kernel(kernel) : nullptr;
+    if (!k) throw lfg::LfError{LF_ERR_BAD_NAME, std::string("Bad Kernel or Solver Name: ") +
+                                                    (kernel ? kernel : "(null)")};
+    int i = b->b->add(k, nd, dims);
+    if (index_out) *index_out = i;
+  });
+}
+
+int lf_batch_size(const lf_batch* b) { return b ? int(b->b->members.size()) : -1; }
+
+int lf_batch_add_energy_potentials(lf_batch* b, int index, const int64_t* unary,
+                                   const int64_t* binary) {
+  return guarded([&] {
+    if (!b || !unary || !binary) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    b->b->add_energy(index, unary, binary);
+  });
+}
+
+int lf_batch_add_capacities(lf_batch* b, int index, const int32_t* src, const int32_t* snk,
+                            const int32_t* edge) {
+  return guarded([&] {
+    if (!b) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    b->b->add_caps(index, src, snk, edge);
+  });
+}
+
+int lf_batch_clear(lf_batch* b) {
+  return guarded([&] {
+    if (!b) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    b->b->clear();
+  });
+}
+
+int lf_batch_run(lf_batch* b) {
+  return guarded([&] {
+    if (!b) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    b->b->run();
+  });
+}
+
+double lf_batch_run_time(const lf_batch* b) { return b ? b->b->run_time : 0.0; }
+
+int lf_batch_get_cut(lf_batch* b, int index, int* out) {
+  return guarded([&] {
+    if (!b || !out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    b->b->get_cut(index, out, false);
+  });
+}
+
+int lf_batch_get_cut_max(lf_batch* b, int index, int* out) {
+  return guarded([&] {
+    if (!b || !out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    b->b->get_cut(index, out, true);
+  });
+}
+
+int lf_batch_get_flow(lf_batch* b, int index, int64_t* flow, int64_t* energy) {
+  return guarded([&] {
+    if (!b) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    if (!b->b->solved) throw lfg::LfError{LF_ERR_STATE, "no solution yet"};
+    lfg::Member& m = b->b->member(index);
+    if (flow) *flow = m.flow;
+    if (energy) *energy = m.energy;
+  });
+}
+
+int lf_batch_set_param(lf_batch* b, const char* name, int value) {
+  return guarded([&] {
+    if (!b || !name) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    std::string n(name);
+    lfg::Tuning& t = b->b->tune;
+    if (n == "tile_rows") t.tile_rows = value;
+    else if (n == "local_sweeps") t.sweeps = value;
+    else if (n == "launches_per_relabel") t.launches_per_relabel = value;
+    else if (n == "height_slack") t.height_slack = value;
+    else if (n == "pass_chunk") t.pass_chunk = value;
+    else if (n == "defer_checks") b->b->defer_checks = value != 0;
+    else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
+  });
+}
+
+int lf_batch_get_stats(const lf_batch* b, int64_t* epochs, int64_t* pr, int64_t* bfs) {
+  if (!b) return LF_ERR_INVALID;
+  if (epochs) *epochs = b->b->stats.epochs;
+  if (pr) *pr = b->b->stats.pr_launches;
+  if (bfs) *bfs = b->b->stats.bfs_passes;
+  return LF_OK;
 }
 
 }  // extern "C"

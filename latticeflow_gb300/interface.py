@@ -283,3 +283,93 @@ def calculate2dTV(f, lam, kernel="Full2d_4", return_levels=False):
     lv = np.empty((nx, ny), dtype=np.int64)
     N.check(N.lib().lf_tv_2d(kernel.encode(), nx, ny, _p(f), float(lam), _p(out), _p(lv)))
     return (out, lv) if return_levels else out
+
+
+class LatticeBatch(object):
+    """Many independent lattices solved together on the GPU (one instance pool).
+
+    ``add(kernel, shape)`` returns the lattice's index; fill each lattice with
+    ``addCapacities`` / ``addEnergyPotentials``; ``run()`` solves all of them;
+    results per index.  Each lattice's result equals a plain ``LatticeFlow``
+    solve of it.
+    """
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        N.check(N.lib().lf_batch_create(ctypes.byref(h)))
+        self._h = h
+        self._shapes = []
+        self._edges = []
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            N.lib().lf_batch_destroy(h)
+            self._h = None
+
+    def __len__(self):
+        return len(self._shapes)
+
+    def add(self, kernel, shape):
+        shape = tuple(int(v) for v in shape)
+        dims = np.asarray(shape, dtype=np.uint64)
+        idx = ctypes.c_int(-1)
+        N.check(N.lib().lf_batch_add(self._h, kernel.encode(), len(shape), _p(dims), ctypes.byref(idx)))
+        self._shapes.append(shape)
+        self._edges.append(kernelInfo(kernel)[0].shape[0] // 2)
+        return idx.value
+
+    def setParam(self, name, value):
+        N.check(N.lib().lf_batch_set_param(self._h, name.encode(), int(value)))
+
+    def addCapacities(self, index, source=None, sink=None, edges=None):
+        n = int(np.prod(self._shapes[index]))
+        arrs = []
+        for a, m in ((source, n), (sink, n), (edges, n * self._edges[index])):
+            if a is None:
+                arrs.append(None)
+                continue
+            a = np.ascontiguousarray(a, dtype=np.int32).reshape(-1)
+            if a.size != m:
+                raise ValueError("capacity array has the wrong size")
+            arrs.append(a)
+        N.check(N.lib().lf_batch_add_capacities(
+            self._h, index, *[(_p(a) if a is not None else None) for a in arrs]))
+
+    def addEnergyPotentials(self, index, unary, binary):
+        n = int(np.prod(self._shapes[index]))
+        u = np.ascontiguousarray(unary, dtype=np.int64).reshape(-1)
+        b = np.ascontiguousarray(binary, dtype=np.int64).reshape(-1)
+        if u.size != 2 * n or b.size != 4 * n * self._edges[index]:
+            raise ValueError("energy arrays do not match the lattice")
+        N.check(N.lib().lf_batch_add_energy_potentials(self._h, index, _p(u), _p(b)))
+
+    def clear(self):
+        N.check(N.lib().lf_batch_clear(self._h))
+
+    def run(self):
+        N.check(N.lib().lf_batch_run(self._h))
+
+    def runTime(self):
+        return N.lib().lf_batch_run_time(self._h)
+
+    def getCut(self, index):
+        out = np.empty(int(np.prod(self._shapes[index])), dtype=np.int32)
+        N.check(N.lib().lf_batch_get_cut(self._h, index, _p(out)))
+        return out.reshape(self._shapes[index])
+
+    def getCutMax(self, index):
+        out = np.empty(int(np.prod(self._shapes[index])), dtype=np.int32)
+        N.check(N.lib().lf_batch_get_cut_max(self._h, index, _p(out)))
+        return out.reshape(self._shapes[index])
+
+    def flow(self, index):
+        f = ctypes.c_int64(0)
+        e = ctypes.c_int64(0)
+        N.check(N.lib().lf_batch_get_flow(self._h, index, ctypes.byref(f), ctypes.byref(e)))
+        return f.value, e.value
+
+    def stats(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        N.check(N.lib().lf_batch_get_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"epochs": a.value, "pr_passes": b.value, "bfs_passes": c.value}
