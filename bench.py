@@ -42,7 +42,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_cut",
-                    choices=["large_cut", "plain_cut", "volume_cut"])
+                    choices=["large_cut", "plain_cut", "volume_cut", "batch"])
+    ap.add_argument("--batch-size", type=int, default=512)
+    ap.add_argument("--no-batch-summary", action="store_true",
+                    help="skip the batched-vs-plain summary of the default run")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--profile-run", action="store_true",
                     help="only warm-up and timed device-resident solves (for ncu captures)")
@@ -226,6 +230,11 @@ def run_ours(args):
         barrier()
         return ms, res, prof, launches
 
+    tuning = None
+    if not args.no_autotune and not args.profile_run:
+        from latticeflow_gb300 import autotune
+        step_device()
+        tuning, _, _ = autotune.tune(L, autotune.problem_key([p.kernel], p.n))
     for _ in range(args.warmup):
         step_device()
     if args.profile_run:
@@ -269,7 +278,8 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generator, latticeflow_gb300/workloads.py)",
-        "config": dict(workload_config(args.workload, p), parallelism="replicas" if world > 1 else "single"),
+        "config": dict(workload_config(args.workload, p), parallelism="replicas" if world > 1 else "single",
+                       tuning=tuning, autotuned=tuning is not None),
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT,
                 "h2d_bytes_per_step": int(u.nbytes + b.nbytes),
                 "d2h_bytes_per_step": int(2 * p.n * 4 + 64)},
@@ -281,10 +291,131 @@ def run_ours(args):
     }
     if rank == 0:
         out["cpu_baseline"] = cpu_baseline(p)
+        if not args.no_batch_summary and not args.profile_run:
+            del L
+            out["batched_vs_plain"] = batch_summary(args)
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def make_batch(count, seed=0):
+    from latticeflow_gb300 import workloads as W
+    return W.batch(count, seed=seed)
+
+
+def fill_batch(B, probs):
+    for i, p in enumerate(probs):
+        B.addCapacities(i, p.source, p.sink, p.edge)
+
+
+def batch_summary(args, steps=3):
+    """Batched (one pool) vs sequential plain solves of the same lattices."""
+    import torch
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import autotune
+    probs = make_batch(args.batch_size)
+    B = lf.LatticeBatch()
+    for p in probs:
+        B.add(p.kernel, p.dims)
+    B.setParam("defer_checks", 1)
+    fill_batch(B, probs)
+    B.run()
+    setting, _, _ = autotune.tune(B, autotune.problem_key([p.kernel for p in probs],
+                                                          sum(p.n for p in probs)))
+    torch.cuda.synchronize()
+    tb = []
+    for _ in range(steps):
+        B.run()
+        tb.append(B.runTime())
+    plain = []
+    for p in probs:
+        L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+        L.addCapacities(p.source, p.sink, p.edge)
+        plain.append(L)
+    for L in plain[:4]:
+        L.run()
+    tp = []
+    for _ in range(max(1, steps - 1)):
+        t = 0.0
+        for L in plain:
+            L.run()
+            t += L.runTime()
+        tp.append(t)
+    mism = sum(1 for i, L in enumerate(plain)
+               if L.flow() != B.flow(i) or not np.array_equal(L.getCut(), B.getCut(i)))
+    n = len(probs)
+    return {"lattices": n, "nodes": int(sum(p.n for p in probs)),
+            "batched_solves_per_s": round(n / min(tb), 2),
+            "plain_solves_per_s": round(n / min(tp), 2),
+            "speedup": round(min(tp) / min(tb), 2), "tuning": setting,
+            "results_differ": mism,
+            "timing": "device time of complete solves (CUDA events), best of %d" % steps}
+
+
+def run_batch(args):
+    """--workload batch: 512 uneven lattices, one pool solve per step."""
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from latticeflow_gb300 import _build
+    _build.build_native()
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import autotune
+    probs = make_batch(args.batch_size, seed=args.seed)
+    B = lf.LatticeBatch()
+    for p in probs:
+        B.add(p.kernel, p.dims)
+    B.setParam("defer_checks", 1)
+    fill_batch(B, probs)
+    B.run()
+    setting = None
+    if not args.no_autotune:
+        setting, _, _ = autotune.tune(B, autotune.problem_key([p.kernel for p in probs],
+                                                              sum(p.n for p in probs)))
+    for _ in range(args.warmup):
+        B.run()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    t0 = time.perf_counter()
+    dev = 0.0
+    for _ in range(args.steps):
+        B.run()
+        dev += B.runTime()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    # e2e: host capacities in, every cut out
+    cut_bytes = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        B.clear()
+        fill_batch(B, probs)
+        B.run()
+        for i in range(len(probs)):
+            cut_bytes += B.getCut(i).nbytes
+    wall_e2e = time.perf_counter() - t0
+    n = len(probs)
+    summary = batch_summary(args) if rank == 0 else None
+    h2d = int(sum(p.source.nbytes + p.sink.nbytes + p.edge.nbytes for p in probs))
+    out = {
+        "metric": METRIC, "value": round(n * args.steps / dev, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dev / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator, latticeflow_gb300/workloads.py)",
+        "config": {"workload": "batch", "lattices": n, "kernels": "Full2d_4 + Full2d_8",
+                   "sides": "log-uniform [64, 1024] per axis", "capacity": "int32",
+                   "tuning": setting, "autotuned": setting is not None,
+                   "l2": "inputs larger than L2 (no flush needed)"},
+        "e2e": {"value": round(n * args.steps / wall_e2e, 3), "unit": UNIT,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(cut_bytes / args.steps)},
+        "wall_ms_per_step": round(1e3 * wall / args.steps, 3),
+        "clocks": clocks,
+        "batched_vs_plain": summary,
+    }
+    if rank == 0:
+        print(json.dumps(out))
 
 
 def cpu_baseline(p, budget_s=12.0):
@@ -307,17 +438,27 @@ def cpu_baseline(p, budget_s=12.0):
 _W = {}
 
 
-def _ref_init(workload, seed):
+def _ref_init(workload, seed, batch_size=512):
     sys.path.insert(0, ROOT)
     from oracle import oracle as O
     O.port()
+    if workload == "batch":
+        _W["batch"] = make_batch(batch_size, seed=seed)
+        return
     p = make_workload(workload, seed)
     _W["p"] = p
     _W["e"] = p.energies()
 
 
-def _ref_solve(_):
+def _ref_solve(arg):
     from oracle import oracle as O
+    if "batch" in _W:
+        secs = 0.0
+        for i in arg:
+            p = _W["batch"][i]
+            _, s = O.port_pr(p.kernel, p.dims, *p.energies())
+            secs += s
+        return secs
     p = _W["p"]
     u, b = _W["e"]
     _, secs = O.port_pr(p.kernel, p.dims, u, b)
@@ -333,15 +474,23 @@ def run_reference(args):
     O.build_port()
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
-    p = make_workload(args.workload, args.seed)
-    with ctx.Pool(cores, initializer=_ref_init, initargs=(args.workload, args.seed)) as pool:
+    if args.workload == "batch":
+        p = None
+        per_step = args.batch_size
+        work = [list(range(c, args.batch_size, cores)) for c in range(cores)]
+    else:
+        p = make_workload(args.workload, args.seed)
+        per_step = cores
+        work = list(range(cores))
+    with ctx.Pool(cores, initializer=_ref_init,
+                  initargs=(args.workload, args.seed, args.batch_size)) as pool:
         for _ in range(args.warmup):
-            pool.map(_ref_solve, range(cores), chunksize=1)
+            pool.map(_ref_solve, work, chunksize=1)
         t0 = time.time()
         for _ in range(args.steps):
-            pool.map(_ref_solve, range(cores), chunksize=1)
+            pool.map(_ref_solve, work, chunksize=1)
         wall = time.time() - t0
-    value = cores * args.steps / wall
+    value = per_step * args.steps / wall
     kind = "port"
     out = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
@@ -349,10 +498,14 @@ def run_reference(args):
         "ms_per_step": round(1e3 * wall / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int64",
         "data": "synthetic (seeded generator, latticeflow_gb300/workloads.py)",
-        "config": workload_config(args.workload, p),
+        "config": workload_config(args.workload, p) if p is not None else
+                  {"workload": "batch", "lattices": args.batch_size},
         "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": kind,
-                         "sample": "each step: one full solve per host core in parallel "
-                                   "(reference push-relabel restated, oracle/lf_oracle.cpp)"},
+                         "sample": ("each step: one full solve per host core in parallel"
+                                    if p is not None else
+                                    "each step: all %d lattices spread over the host cores"
+                                    % args.batch_size) +
+                                   " (reference push-relabel restated, oracle/lf_oracle.cpp)"},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -363,6 +516,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

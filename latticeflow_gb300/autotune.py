@@ -1,0 +1,93 @@
+"""Autotuner for the solve knobs: tile shape, local sweeps, launches per relabel.
+
+The knobs trade tile occupancy (tile rows), work per tile visit (local
+push/relabel sweeps) and global-relabel frequency (push/relabel passes
+between two global relabels).  Their best values depend on the kernel and the
+lattice sizes, so they are measured: every candidate is timed on the actual
+problem (device time of complete solves, best of ``repeats``), the fastest is
+applied and remembered per key (kernel set and size class) in memory and,
+when ``cache_path`` is given, in a JSON file.  Results do not depend on the
+knobs (the cut sets are canonical), only the time does.
+"""
+import itertools
+import json
+import math
+import os
+
+DEFAULT_GRID = {
+    "tile_rows": (16, 32),
+    "local_sweeps": (2, 4, 8),
+    "launches_per_relabel": (2, 4, 8),
+}
+
+_memory = {}
+
+
+def size_class(n_nodes):
+    """log2 bucket of the node count."""
+    return int(math.floor(math.log2(max(1, n_nodes))))
+
+
+def problem_key(kernels, n_nodes):
+    return "%s|%d" % ("+".join(sorted(set(kernels))), size_class(n_nodes))
+
+
+def _load(cache_path):
+    if cache_path and os.path.exists(cache_path):
+        with open(cache_path) as f:
+            return json.load(f)
+    return {}
+
+
+def _store(cache_path, table):
+    if not cache_path:
+        return
+    d = os.path.dirname(cache_path)
+    if d:
+        os.makedirs(d, exist_ok=True)
+    tmp = cache_path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+    os.replace(tmp, cache_path)
+
+
+def tune(solver, key, grid=None, repeats=2, cache_path=None, force=False):
+    """Choose and apply the fastest knob setting for ``solver``.
+
+    ``solver`` is a ``LatticeFlow`` or ``LatticeBatch`` that is already
+    filled; it must offer ``setParam``, ``run`` and ``runTime``.  Returns
+    (setting, seconds, table of all timings).
+    """
+    table = dict(_memory)
+    table.update(_load(cache_path))
+    if not force and key in table:
+        best = table[key]["setting"]
+        for k, v in best.items():
+            solver.setParam(k, v)
+        return best, table[key]["seconds"], None
+    grid = grid or DEFAULT_GRID
+    names = sorted(grid)
+    timings = []
+    best, best_t = None, float("inf")
+    for values in itertools.product(*[grid[n] for n in names]):
+        setting = dict(zip(names, values))
+        for k, v in setting.items():
+            solver.setParam(k, v)
+        t = min(_timed(solver) for _ in range(repeats))
+        timings.append((setting, t))
+        if t < best_t:
+            best, best_t = setting, t
+    for k, v in best.items():
+        solver.setParam(k, v)
+    entry = {"setting": best, "seconds": best_t}
+    _memory[key] = entry
+    if cache_path:
+        disk = _load(cache_path)
+        disk[key] = entry
+        _store(cache_path, disk)
+    return best, best_t, timings
+
+
+def _timed(solver):
+    solver.run()
+    return solver.runTime()

@@ -34,6 +34,7 @@ class Batch {
   void run();
   void get_cut(int i, int* out, bool maximal);
   Member& member(int i);
+  void relayout() { runner_ready = false; }
 
   std::vector<Member> members;
   Tuning tune;

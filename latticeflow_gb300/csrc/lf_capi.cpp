@@ -385,7 +385,7 @@ int lf_batch_set_param(lf_batch* b, const char* name, int value) {
     if (!b || !name) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
     std::string n(name);
     lfg::Tuning& t = b->b->tune;
-    if (n == "tile_rows") t.tile_rows = value;
+    if (n == "tile_rows") { t.tile_rows = value; b->b->relayout(); }
     else if (n == "local_sweeps") t.sweeps = value;
     else if (n == "launches_per_relabel") t.launches_per_relabel = value;
     else if (n == "height_slack") t.height_slack = value;
