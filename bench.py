@@ -258,9 +258,9 @@ def run_ours(args):
     pr_bytes = prof["pr_tiles"] * nt * 2 * (K * elem + elem + 4)
     bfs_bytes = prof["bfs_tiles"] * nt * (8 + 4 + 4)
     if prof["pr_ms"] >= prof["bfs_ms"]:
-        kname, kbytes, kms, klaunch = "k_pr_tile", pr_bytes, prof["pr_ms"], prof["pr_launches"]
+        kname, kbytes, kms, klaunch = "k_pool_pr", pr_bytes, prof["pr_ms"], prof["pr_launches"]
     else:
-        kname, kbytes, kms, klaunch = "k_bfs_tile", bfs_bytes, prof["bfs_ms"], prof["bfs_passes"]
+        kname, kbytes, kms, klaunch = "k_pool_bfs", bfs_bytes, prof["bfs_ms"], prof["bfs_passes"]
     achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else 0.0
     tr = committed_traffic(args.workload + ":" + kname)
     roofline = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1),
