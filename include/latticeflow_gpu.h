@@ -179,6 +179,28 @@ int lf_batch_set_param(lf_batch* b, const char* name, int value);
 /* epochs, push/relabel passes, BFS passes of the last run */
 int lf_batch_get_stats(const lf_batch* b, int64_t* epochs, int64_t* pr_passes, int64_t* bfs_passes);
 
+/* ------------------------------------------------------ no allocation
+ * No counterpart in the reference.  A binary cut of one small 2-d lattice
+ * (Full2d_4 / Full2d_8 and their Star aliases, int32 capacities) that
+ * allocates no memory: for callers that must not allocate device memory
+ * while they run -- code living inside another framework's memory budget or
+ * pool, real-time or embedded hosts that forbid allocation after start-up,
+ * plugins whose host process owns every allocation.  Inputs and outputs are
+ * the caller's DEVICE buffers: source/sink[nx*ny] and edge[nx*ny*(K/2)]
+ * capacities as lf_add_capacities, cut[nx*ny] receives the minimal on-set
+ * (as lf_get_cut), flow_energy[2] the flow value and the minimum energy.
+ * All intermediate state lives in one static device array of 8.5 MiB per GPU,
+ * enough for 65,536 padded nodes (sides rounded up to 32, e.g. 256 x 256);
+ * larger lattices return LF_ERR_RANGE.  The first call on a device looks the
+ * array's address up (make that first call before any stream capture).  The
+ * array is shared by all calls and keeps the last call's contents; each call
+ * clears what must start at zero.  Calls whose GPU work overlapped would race
+ * on it: the call holds a process-wide lock and synchronises `stream` (a
+ * cudaStream_t, NULL = legacy default stream) before returning. */
+int lf_cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* source_device,
+                      const int32_t* sink_device, const int32_t* edge_device,
+                      int32_t* cut_device, int64_t* flow_energy_device, void* stream);
+
 /* ------------------------------------------------------------------- TV
  * calculate2dTV<Kernel, int64>(nx, ny, f, lambda) (tv/tv_solver.hpp:650-655):
  * the single-lambda TV solve on the GPU.  f, out: nx*ny doubles, row-major.

@@ -60,6 +60,7 @@ PROTOTYPES = {
     "lf_batch_get_flow": (I, [P, I, P, P]),
     "lf_batch_set_param": (I, [P, ctypes.c_char_p, I]),
     "lf_batch_get_stats": (I, [P, P, P, P]),
+    "lf_cut_2d_noalloc": (I, [ctypes.c_char_p, SZ, SZ, P, P, P, P, P, P]),
 }
 
 LF_OK = 0

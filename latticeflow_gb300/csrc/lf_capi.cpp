@@ -288,6 +288,16 @@ int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double l
   });
 }
 
+// ------------------------------------------------------------ no allocation
+
+int lf_cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* src,
+                      const int32_t* snk, const int32_t* edge, int32_t* cut, int64_t* fe,
+                      void* stream) {
+  return guarded([&] {
+    lfg::cut_2d_noalloc(kernel, nx, ny, src, snk, edge, cut, fe, (cudaStream_t)stream);
+  });
+}
+
 // ----------------------------------------------------------------- batches
 
 int lf_batch_create(lf_batch** out) {

@@ -106,6 +106,9 @@ class Engine : public ProfHooks {
 };
 
 void engine_run_parametric(Engine& E);  // lf_param.cu
+int cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* src,
+                   const int32_t* snk, const int32_t* edge, int32_t* cut, int64_t* flow_energy,
+                   cudaStream_t s);  // lf_noalloc.cu
 int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lambda, double* out,
           int64_t* levels_out);
 

@@ -199,6 +199,70 @@ int occupancy_grid(K kernel, int threads, size_t smem) {
 
 size_t pool_smem_head_bytes() { return sizeof(PoolSmemHead); }
 
+// Launchers of the node-level pool kernels (used by PoolRunner and by the
+// allocation-free single-lattice driver).
+template <typename T>
+cudaError_t pool_init_heights(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                              const T* exc, const uint64_t* kmask, int* h, cudaStream_t s) {
+  k_pool_init_heights<T><<<nblk(NP, 256), 256, 0, s>>>(insts, nbase, n, NP, exc, kmask, h);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t pool_mask(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                      const T* res, const uint64_t* kmask, uint64_t* mask, cudaStream_t s) {
+  k_pool_mask<T><<<nblk(NP, 256), 256, 0, s>>>(insts, nbase, n, NP, res, kmask, mask);
+  return cudaGetLastError();
+}
+cudaError_t pool_queue_all(const InstDesc* insts, const int* tile_inst, int tiles, TileQueue q,
+                           cudaStream_t s) {
+  if (tiles > 0) k_pool_queue_all<<<nblk(tiles, 256), 256, 0, s>>>(insts, tile_inst, tiles, q);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t pool_active(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                        const T* exc, const int* h, TileQueue q, unsigned long long* cnt,
+                        unsigned* hmx, cudaStream_t s) {
+  k_pool_active<T><<<nblk(NP, 256), 256, 0, s>>>(insts, nbase, n, NP, exc, h, q, cnt, hmx);
+  return cudaGetLastError();
+}
+cudaError_t pool_update(InstDesc* insts, int n, const unsigned long long* cnt, const unsigned* hmx,
+                        long long cap, int slack, unsigned long long* total, cudaStream_t s) {
+  k_pool_update<<<nblk(n, 256), 256, 0, s>>>(insts, n, cnt, hmx, cap, slack, total);
+  return cudaGetLastError();
+}
+cudaError_t pool_reset(InstDesc* insts, int n, cudaStream_t s) {
+  k_pool_reset<<<nblk(n, 256), 256, 0, s>>>(insts, n);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t pool_init_marks(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                            const T* exc, int* mark, cudaStream_t s) {
+  k_pool_init_marks<T><<<nblk(NP, 256), 256, 0, s>>>(insts, nbase, n, NP, exc, mark);
+  return cudaGetLastError();
+}
+cudaError_t pool_queue_active(const InstDesc* insts, const int* tile_inst, int tiles, TileQueue q,
+                              cudaStream_t s) {
+  if (tiles > 0) k_pool_queue_active<<<nblk(tiles, 256), 256, 0, s>>>(insts, tile_inst, tiles, q);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t pool_sum_pos(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                         const T* exc, long long* sums, cudaStream_t s) {
+  k_pool_sum_pos<T><<<nblk(NP, 256), 256, 0, s>>>(insts, nbase, n, NP, exc, sums);
+  return cudaGetLastError();
+}
+template cudaError_t pool_init_heights<int>(const InstDesc*, const long long*, int, long long,
+                                            const int*, const uint64_t*, int*, cudaStream_t);
+template cudaError_t pool_mask<int>(const InstDesc*, const long long*, int, long long, const int*,
+                                    const uint64_t*, uint64_t*, cudaStream_t);
+template cudaError_t pool_active<int>(const InstDesc*, const long long*, int, long long, const int*,
+                                      const int*, TileQueue, unsigned long long*, unsigned*,
+                                      cudaStream_t);
+template cudaError_t pool_init_marks<int>(const InstDesc*, const long long*, int, long long,
+                                          const int*, int*, cudaStream_t);
+template cudaError_t pool_sum_pos<int>(const InstDesc*, const long long*, int, long long,
+                                       const int*, long long*, cudaStream_t);
+
 // ------------------------------------------------------------------ runner
 
 void PoolRunner::check(cudaError_t e, const char* what) {

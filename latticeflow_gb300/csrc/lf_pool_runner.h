@@ -52,6 +52,30 @@ cudaError_t launch_pool_bfs(const PoolBFS& p, int KA, int KB, bool single, int g
 cudaError_t launch_pool_reach(const PoolReach& p, int KA, int KB, bool single, int grid,
                               int threads, size_t smem, cudaStream_t s);
 
+template <typename T>
+cudaError_t pool_init_heights(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                              const T* exc, const uint64_t* kmask, int* h, cudaStream_t s);
+template <typename T>
+cudaError_t pool_mask(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                      const T* res, const uint64_t* kmask, uint64_t* mask, cudaStream_t s);
+cudaError_t pool_queue_all(const InstDesc* insts, const int* tile_inst, int tiles, TileQueue q,
+                           cudaStream_t s);
+template <typename T>
+cudaError_t pool_active(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                        const T* exc, const int* h, TileQueue q, unsigned long long* cnt,
+                        unsigned* hmx, cudaStream_t s);
+cudaError_t pool_update(InstDesc* insts, int n, const unsigned long long* cnt, const unsigned* hmx,
+                        long long cap, int slack, unsigned long long* total, cudaStream_t s);
+cudaError_t pool_reset(InstDesc* insts, int n, cudaStream_t s);
+template <typename T>
+cudaError_t pool_init_marks(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                            const T* exc, int* mark, cudaStream_t s);
+cudaError_t pool_queue_active(const InstDesc* insts, const int* tile_inst, int tiles, TileQueue q,
+                              cudaStream_t s);
+template <typename T>
+cudaError_t pool_sum_pos(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                         const T* exc, long long* sums, cudaStream_t s);
+
 class PoolRunner {
  public:
   ~PoolRunner();
