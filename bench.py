@@ -42,7 +42,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_cut",
-                    choices=["large_cut", "plain_cut", "volume_cut", "batch"])
+                    choices=["large_cut", "plain_cut", "volume_cut", "batch", "serve"])
+    ap.add_argument("--requests", type=int, default=200, help="serve: measured requests")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
+    ap.add_argument("--workers", type=int, default=4, help="serve: server workers")
     ap.add_argument("--batch-size", type=int, default=512)
     ap.add_argument("--no-batch-summary", action="store_true",
                     help="skip the batched-vs-plain summary of the default run")
@@ -418,6 +421,74 @@ def run_batch(args):
         print(json.dumps(out))
 
 
+SERVE_SIZES = (128, 256, 512, 1024, 2048)
+
+
+def run_serve(args):
+    """--workload serve: Poisson stream of single-lambda TV requests, sizes
+    uniform over {128..2048}^2, lambda log-uniform in [1e-3, 1]."""
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    from latticeflow_gb300 import _build
+    _build.build_native()
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    rng = np.random.default_rng(args.seed)
+    images = {n: W.tv_image(100 + i, n=n, polygons=30) for i, n in enumerate(SERVE_SIZES)}
+    S = lf.LatticeServer(workers=args.workers)
+    # warm-up: every size once per worker (engines and kernels loaded)
+    warm = [S.submit_tv(images[n], 0.01) for n in SERVE_SIZES for _ in range(args.workers)]
+    for t in warm:
+        S.wait(t)
+        S.release(t)
+    sizes = rng.choice(SERVE_SIZES, size=args.requests)
+    lams = np.exp(rng.uniform(np.log(1e-3), np.log(1.0), size=args.requests))
+    gaps = rng.exponential(1.0 / args.rate, size=args.requests)
+    arrive = np.cumsum(gaps)
+    tickets = []
+    sampler = ClockSampler(local)
+    sampler.start()
+    t0 = time.perf_counter()
+    for i in range(args.requests):
+        delay = t0 + arrive[i] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        tickets.append(S.submit_tv(images[int(sizes[i])], float(lams[i])))
+    lat = []
+    for t in tickets:
+        lat.append(S.wait(t))
+        S.release(t)
+    makespan = time.perf_counter() - t0
+    clocks = sampler.stop()
+    st = S.stats()
+    S.close()
+    lat_ms = np.sort(np.asarray(lat) * 1e3)
+    per_size = {}
+    for n in SERVE_SIZES:
+        m = sizes == n
+        if m.any():
+            l = np.asarray(lat)[m] * 1e3
+            per_size[str(n)] = {"count": int(m.sum()), "p50_ms": round(float(np.percentile(l, 50)), 2),
+                                "p99_ms": round(float(np.percentile(l, 99)), 2)}
+    out = {
+        "metric": METRIC, "value": round(args.requests / makespan, 3), "unit": "solves/s",
+        "n_gpus": world, "steps": args.requests, "warmup": len(warm),
+        "ms_per_step": round(1e3 * makespan / args.requests, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+        "data": "synthetic (seeded polygon images, latticeflow_gb300/workloads.py)",
+        "config": {"workload": "serve", "requests": args.requests, "rate_per_s": args.rate,
+                   "sizes": list(SERVE_SIZES), "lambda": "log-uniform [1e-3, 1]",
+                   "kernel": "Full2d_4", "workers": args.workers},
+        "latency_ms": {"p50": round(float(np.percentile(lat_ms, 50)), 2),
+                       "p99": round(float(np.percentile(lat_ms, 99)), 2),
+                       "max": round(float(lat_ms[-1]), 2)},
+        "per_size": per_size, "max_in_flight": st["max_in_flight"], "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def cpu_baseline(p, budget_s=12.0):
     """Restated reference push-relabel on one host core, same workload."""
     from oracle import oracle as O
@@ -518,6 +589,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 

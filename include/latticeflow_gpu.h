@@ -179,6 +179,33 @@ int lf_batch_set_param(lf_batch* b, const char* name, int value);
 /* epochs, push/relabel passes, BFS passes of the last run */
 int lf_batch_get_stats(const lf_batch* b, int64_t* epochs, int64_t* pr_passes, int64_t* bfs_passes);
 
+/* -------------------------------------------------------------- serving
+ * No reference counterpart.  A request server for TV-denoise (single lambda)
+ * and graph-cut requests of any 2-d size: requests are queued as submitted
+ * and admitted when a worker is idle and their device footprint fits in the
+ * HBM budget still free (budget 0 = half the free device memory; a request
+ * larger than the budget runs alone).  Admitted requests run concurrently
+ * on the workers' own CUDA streams, so their kernels overlap on the device;
+ * each worker keeps the engines of the shapes it has served.  Inputs are
+ * copied at submission; results stay until lf_server_release.  Latency =
+ * completion - submission (queueing included). */
+typedef struct lf_server lf_server;
+int lf_server_create(int workers, size_t hbm_budget_bytes, lf_server** out);
+void lf_server_destroy(lf_server* s);
+int lf_server_submit_tv(lf_server* s, const char* kernel, size_t nx, size_t ny, const double* f,
+                        double lambda, int64_t* ticket);
+int lf_server_submit_cut(lf_server* s, const char* kernel, size_t nx, size_t ny,
+                         const int32_t* source, const int32_t* sink, const int32_t* edge,
+                         int64_t* ticket);
+/* LF_OK when finished (latency_s set), LF_ERR_STATE on timeout, else the
+ * request's own error. */
+int lf_server_wait(lf_server* s, int64_t ticket, double timeout_s, double* latency_s);
+int lf_server_get_tv(lf_server* s, int64_t ticket, double* out, int64_t* levels);
+int lf_server_get_cut(lf_server* s, int64_t ticket, int* cut, int64_t* flow, int64_t* energy);
+int lf_server_release(lf_server* s, int64_t ticket);
+int lf_server_stats(lf_server* s, double* p50_ms, double* p99_ms, double* solves_per_s,
+                    int64_t* completed, int64_t* max_in_flight);
+
 /* ------------------------------------------------------ no allocation
  * No counterpart in the reference.  A binary cut of one small 2-d lattice
  * (Full2d_4 / Full2d_8 and their Star aliases, int32 capacities) that

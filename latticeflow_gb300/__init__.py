@@ -5,6 +5,6 @@ The compute path is the native library ``_lib/liblatticeflow_gpu.so`` (CUDA
 for sm_103a, C ABI in ``include/latticeflow_gpu.h``); this package is its
 Python surface.
 """
-from .interface import (LatticeBatch, LatticeFlow, calculate2dTV, isValidKernel, isValidSolver,  # noqa: F401
+from .interface import (LatticeBatch, LatticeFlow, LatticeServer, calculate2dTV, isValidKernel, isValidSolver,  # noqa: F401
                         kernelDimension, kernelInfo, validKernelNames, validSolverNames)
 from ._native import BadSolverOrKernelName, LatticeFlowError, NativeLibraryMissing  # noqa: F401

@@ -61,6 +61,15 @@ PROTOTYPES = {
     "lf_batch_set_param": (I, [P, ctypes.c_char_p, I]),
     "lf_batch_get_stats": (I, [P, P, P, P]),
     "lf_cut_2d_noalloc": (I, [ctypes.c_char_p, SZ, SZ, P, P, P, P, P, P]),
+    "lf_server_create": (I, [I, SZ, P]),
+    "lf_server_destroy": (None, [P]),
+    "lf_server_submit_tv": (I, [P, ctypes.c_char_p, SZ, SZ, P, ctypes.c_double, P]),
+    "lf_server_submit_cut": (I, [P, ctypes.c_char_p, SZ, SZ, P, P, P, P]),
+    "lf_server_wait": (I, [P, ctypes.c_int64, ctypes.c_double, P]),
+    "lf_server_get_tv": (I, [P, ctypes.c_int64, P, P]),
+    "lf_server_get_cut": (I, [P, ctypes.c_int64, P, P, P]),
+    "lf_server_release": (I, [P, ctypes.c_int64]),
+    "lf_server_stats": (I, [P, P, P, P, P, P]),
 }
 
 LF_OK = 0

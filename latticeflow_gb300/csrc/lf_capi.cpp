@@ -6,6 +6,7 @@
 
 #include "../../include/latticeflow_gpu.h"
 #include "lf_batch.h"
+#include "lf_serve.h"
 
 struct lf_lattice {
   lfg::Engine* e;
@@ -13,6 +14,10 @@ struct lf_lattice {
 
 struct lf_batch {
   lfg::Batch* b;
+};
+
+struct lf_server {
+  lfg::Server* s;
 };
 
 namespace lfg {
@@ -285,6 +290,95 @@ int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double l
     if (!f || !out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
     int rc = lfg::tv_2d(k, nx, ny, f, lambda, out, levels_out);
     if (rc) throw lfg::LfError{rc, "tv solve failed"};
+  });
+}
+
+// ------------------------------------------------------------------ serving
+
+int lf_server_create(int workers, size_t budget, lf_server** out) {
+  return guarded([&] {
+    if (!out) throw lfg::LfError{LF_ERR_INVALID, "null output handle"};
+    *out = nullptr;
+    lf_server* h = new lf_server;
+    try {
+      h->s = new lfg::Server(workers, budget);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+void lf_server_destroy(lf_server* s) {
+  if (!s) return;
+  delete s->s;
+  delete s;
+}
+
+int lf_server_submit_tv(lf_server* s, const char* kernel, size_t nx, size_t ny, const double* f,
+                        double lambda, int64_t* ticket) {
+  return guarded([&] {
+    if (!s || !f || !ticket) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    const lfg::KernelDef* k = kernel ? lfg::find_kernel(kernel) : nullptr;
+    if (!k) throw lfg::LfError{LF_ERR_BAD_NAME, std::string("Bad Kernel or Solver Name: ") +
+                                                    (kernel ? kernel : "(null)")};
+    *ticket = s->s->submit_tv(k, nx, ny, f, lambda);
+  });
+}
+
+int lf_server_submit_cut(lf_server* s, const char* kernel, size_t nx, size_t ny,
+                         const int32_t* src, const int32_t* snk, const int32_t* edge,
+                         int64_t* ticket) {
+  return guarded([&] {
+    if (!s || !src || !snk || !edge || !ticket) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    const lfg::KernelDef* k = kernel ? lfg::find_kernel(kernel) : nullptr;
+    if (!k) throw lfg::LfError{LF_ERR_BAD_NAME, std::string("Bad Kernel or Solver Name: ") +
+                                                    (kernel ? kernel : "(null)")};
+    *ticket = s->s->submit_cut(k, nx, ny, src, snk, edge);
+  });
+}
+
+int lf_server_wait(lf_server* s, int64_t ticket, double timeout_s, double* latency_s) {
+  return guarded([&] {
+    if (!s) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    if (!s->s->wait(ticket, timeout_s, latency_s))
+      throw lfg::LfError{LF_ERR_STATE, "request not finished within the timeout"};
+  });
+}
+
+int lf_server_get_tv(lf_server* s, int64_t ticket, double* out, int64_t* levels) {
+  return guarded([&] {
+    if (!s) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    s->s->get_tv(ticket, out, levels);
+  });
+}
+
+int lf_server_get_cut(lf_server* s, int64_t ticket, int* cut, int64_t* flow, int64_t* energy) {
+  return guarded([&] {
+    if (!s) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    long long f = 0, e = 0;
+    s->s->get_cut(ticket, cut, &f, &e);
+    if (flow) *flow = f;
+    if (energy) *energy = e;
+  });
+}
+
+int lf_server_release(lf_server* s, int64_t ticket) {
+  return guarded([&] {
+    if (!s) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    s->s->release(ticket);
+  });
+}
+
+int lf_server_stats(lf_server* s, double* p50, double* p99, double* sps, int64_t* completed,
+                    int64_t* max_in_flight) {
+  return guarded([&] {
+    if (!s) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    long long c = 0, m = 0;
+    s->s->stats(p50, p99, sps, &c, &m);
+    if (completed) *completed = c;
+    if (max_in_flight) *max_in_flight = m;
   });
 }
 

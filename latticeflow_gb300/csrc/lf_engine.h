@@ -111,5 +111,6 @@ int cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* src,
                    cudaStream_t s);  // lf_noalloc.cu
 int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lambda, double* out,
           int64_t* levels_out);
+int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* levels_out);
 
 }  // namespace lfg

@@ -190,10 +190,22 @@ __global__ void k_pf_levels(Geo g, int nd, long long N, const long long* exc, in
   r[b] = -exc[((long long)a * g.Bp + bb) * g.Cp + c];
 }
 
+// Stream-ordered temporary device buffer (no device-wide synchronisation,
+// so concurrent solves on other streams keep running).
 template <class T>
 struct DevBuf {
   T* p = nullptr;
-  ~DevBuf() { if (p) cudaFree(p); }
+  cudaStream_t s = nullptr;
+  void alloc(size_t count, cudaStream_t st) {
+    s = st;
+    cudaError_t e = cudaMallocAsync(&p, count * sizeof(T), st);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw LfError{e == cudaErrorMemoryAllocation ? 5 : 6,
+                    std::string("cudaMallocAsync: ") + cudaGetErrorString(e)};
+    }
+  }
+  ~DevBuf() { if (p) cudaFreeAsync(p, s); }
 };
 
 }  // namespace
@@ -223,18 +235,19 @@ void engine_run_parametric(Engine& E) {
   DevBuf<unsigned long long> lo, hi, cnt, cnt2;
   DevBuf<unsigned char> fin;
   DevBuf<int> child;
-  E.check(cudaMalloc(&key.p, NP * sizeof(int)), "cudaMalloc");
-  E.check(cudaMalloc(&off_old.p, cap_sections * sizeof(long long)), "cudaMalloc");
-  E.check(cudaMalloc(&off_new.p, cap_sections * sizeof(long long)), "cudaMalloc");
-  E.check(cudaMalloc(&rmin.p, cap_sections * sizeof(long long)), "cudaMalloc");
-  E.check(cudaMalloc(&rmax.p, cap_sections * sizeof(long long)), "cudaMalloc");
-  E.check(cudaMalloc(&lo.p, cap_sections * sizeof(unsigned long long)), "cudaMalloc");
-  E.check(cudaMalloc(&hi.p, cap_sections * sizeof(unsigned long long)), "cudaMalloc");
-  E.check(cudaMalloc(&cnt.p, cap_sections * sizeof(unsigned long long)), "cudaMalloc");
-  E.check(cudaMalloc(&cnt2.p, 2 * cap_sections * sizeof(unsigned long long)), "cudaMalloc");
-  E.check(cudaMalloc(&fin.p, cap_sections), "cudaMalloc");
-  E.check(cudaMalloc(&child.p, 2 * cap_sections * sizeof(int)), "cudaMalloc");
+  key.alloc(NP, s);
+  off_old.alloc(cap_sections, s);
+  off_new.alloc(cap_sections, s);
+  rmin.alloc(cap_sections, s);
+  rmax.alloc(cap_sections, s);
+  lo.alloc(cap_sections, s);
+  hi.alloc(cap_sections, s);
+  cnt.alloc(cap_sections, s);
+  cnt2.alloc(2 * cap_sections, s);
+  fin.alloc(cap_sections, s);
+  child.alloc(2 * cap_sections, s);
   if (!E.d_kmask) E.check(cudaMalloc(&E.d_kmask, NP * sizeof(uint64_t)), "cudaMalloc kmask");
+  // (the section mask stays allocated with the engine for its next solve)
 
   E.check(cudaEventRecord(E.ev0, s), "event");
   k_pf_init_keys<<<nblk(NP, 256), 256, 0, s>>>(g, key.p);
@@ -319,7 +332,7 @@ void engine_run_parametric(Engine& E) {
   E.levels_host.assign((size_t)E.N, 0);
   if (E.N > 0) {
     DevBuf<int64_t> r;
-    E.check(cudaMalloc(&r.p, E.N * sizeof(int64_t)), "cudaMalloc");
+    r.alloc(E.N, s);
     k_pf_levels<<<nblk(E.N, 256), 256, 0, s>>>(g, E.nd, E.N, exc, r.p);
     E.check(E.counted(cudaGetLastError()), "pf levels");
     E.check(cudaMemcpyAsync(E.levels_host.data(), r.p, E.N * 8, cudaMemcpyDeviceToHost, s), "memcpy");
@@ -329,14 +342,14 @@ void engine_run_parametric(Engine& E) {
   cudaEventElapsedTime(&ms, E.ev0, E.ev1);
   E.run_time = ms * 1e-3;
   E.prof_ms[3] = ms;
-  cudaFree(E.d_kmask);
-  E.d_kmask = nullptr;
   E.solved = true;
 }
 
 // calculate2dTV<Kernel, int64>(nx, ny, f, lambda)  (tv/tv_solver.hpp:650-655)
-int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lambda, double* out,
-          int64_t* levels_out) {
+// on an existing parametric engine of shape (nx, ny) (its buffers are reused).
+int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* levels_out) {
+  const KernelDef* kd = E.kd;
+  const size_t nx = E.dims[0], ny = E.dims[1];
   const int nbits = 40;  // n_bits_function_precision for int64 (pf_flow_node.hpp:103-115)
   const double fscale = double(int64_t(1) << nbits);
   const size_t N = nx * ny;
@@ -360,13 +373,11 @@ int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lam
   for (int k = 0; k < kd->K; ++k)
     pwf2[k] = 2LL * (long long)std::round((gsv * kd->weight[k]) / scale * fscale);
 
-  size_t dims[2] = {nx, ny};
-  Engine E("GPULevelReductions", kd, 2, dims);
   E.alloc_accumulators();
   DevBuf<int64_t> d_uf;
   DevBuf<long long> d_pwf;
-  E.check(cudaMalloc(&d_uf.p, N * sizeof(int64_t)), "cudaMalloc");
-  E.check(cudaMalloc(&d_pwf.p, kd->K * sizeof(long long)), "cudaMalloc");
+  d_uf.alloc(N, E.stream);
+  d_pwf.alloc(kd->K, E.stream);
   E.check(cudaMemcpyAsync(d_uf.p, uf.data(), N * 8, cudaMemcpyHostToDevice, E.stream), "memcpy");
   E.check(cudaMemcpyAsync(d_pwf.p, pwf2.data(), kd->K * 8, cudaMemcpyHostToDevice, E.stream), "memcpy");
   k_fill_tv<<<nblk((long long)N, 256), 256, 0, E.stream>>>(E.g, E.st, 2, (long long)N, d_uf.p,
@@ -386,6 +397,14 @@ int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lam
   }
   for (size_t i = 0; i < N; ++i) out[i] = (R[i] - sum / double(N)) * scale + mean;
   return 0;
+}
+
+int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lambda, double* out,
+          int64_t* levels_out) {
+  if (nx * ny == 0) return 0;
+  size_t dims[2] = {nx, ny};
+  Engine E("GPULevelReductions", kd, 2, dims);
+  return tv_2d_on(E, f, lambda, out, levels_out);
 }
 
 }  // namespace lfg

@@ -373,3 +373,79 @@ class LatticeBatch(object):
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         N.check(N.lib().lf_batch_get_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return {"epochs": a.value, "pr_passes": b.value, "bfs_passes": c.value}
+
+
+class LatticeServer(object):
+    """Request server: TV-denoise and graph-cut requests admitted as they
+    arrive and solved concurrently on the GPU (see ``lf_server_*``).
+
+    ``submit_tv`` / ``submit_cut`` return a ticket at once; ``wait`` blocks
+    until the request is finished and returns its latency in seconds;
+    ``result`` returns the solution.  ``stats()`` gives p50 / p99 latency,
+    throughput and the largest number of requests in flight together.
+    """
+
+    def __init__(self, workers=4, hbm_budget_bytes=0):
+        h = ctypes.c_void_p()
+        N.check(N.lib().lf_server_create(int(workers), int(hbm_budget_bytes), ctypes.byref(h)))
+        self._h = h
+        self._meta = {}
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h:
+            N.lib().lf_server_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def submit_tv(self, f, lam, kernel="Full2d_4"):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        t = ctypes.c_int64(0)
+        N.check(N.lib().lf_server_submit_tv(self._h, kernel.encode(), f.shape[0], f.shape[1],
+                                            _p(f), float(lam), ctypes.byref(t)))
+        self._meta[t.value] = ("tv", f.shape)
+        return t.value
+
+    def submit_cut(self, kernel, shape, source, sink, edges):
+        s = np.ascontiguousarray(source, dtype=np.int32).reshape(-1)
+        k = np.ascontiguousarray(sink, dtype=np.int32).reshape(-1)
+        e = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1)
+        t = ctypes.c_int64(0)
+        N.check(N.lib().lf_server_submit_cut(self._h, kernel.encode(), shape[0], shape[1], _p(s),
+                                             _p(k), _p(e), ctypes.byref(t)))
+        self._meta[t.value] = ("cut", tuple(shape))
+        return t.value
+
+    def wait(self, ticket, timeout=600.0):
+        lat = ctypes.c_double(0)
+        N.check(N.lib().lf_server_wait(self._h, ctypes.c_int64(ticket), float(timeout),
+                                       ctypes.byref(lat)))
+        return lat.value
+
+    def result(self, ticket):
+        kind, shape = self._meta[ticket]
+        if kind == "tv":
+            out = np.empty(shape, dtype=np.float64)
+            lv = np.empty(shape, dtype=np.int64)
+            N.check(N.lib().lf_server_get_tv(self._h, ctypes.c_int64(ticket), _p(out), _p(lv)))
+            return out, lv
+        cut = np.empty(shape, dtype=np.int32)
+        f = ctypes.c_int64(0)
+        e = ctypes.c_int64(0)
+        N.check(N.lib().lf_server_get_cut(self._h, ctypes.c_int64(ticket), _p(cut), ctypes.byref(f),
+                                          ctypes.byref(e)))
+        return cut, (f.value, e.value)
+
+    def release(self, ticket):
+        N.check(N.lib().lf_server_release(self._h, ctypes.c_int64(ticket)))
+        self._meta.pop(ticket, None)
+
+    def stats(self):
+        p50, p99, sps = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        c, m = ctypes.c_int64(), ctypes.c_int64()
+        N.check(N.lib().lf_server_stats(self._h, ctypes.byref(p50), ctypes.byref(p99),
+                                        ctypes.byref(sps), ctypes.byref(c), ctypes.byref(m)))
+        return {"p50_ms": p50.value, "p99_ms": p99.value, "solves_per_s": sps.value,
+                "completed": c.value, "max_in_flight": m.value}
