@@ -438,7 +438,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   const int KA = ka, KB = kb;
   const int NTmax = threads;
   const size_t smem = pool_pr_smem<T>(KB, NTmax, hv_max);
-  const long long max_epochs = 20000;
+  const long long max_epochs = 1000000;
   const auto t0 = std::chrono::steady_clock::now();
   for (long long epoch = 0;; ++epoch) {
     if (epoch > max_epochs) throw LfError{4, "push-relabel did not converge"};
@@ -467,8 +467,8 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   if (sets) reach<T>(exc, mask, markv, stats);
   unsigned long long c[2];
   sync_read(c, d_counters, sizeof(c));
-  stats.tiles_processed = c[0];
-  stats.bfs_tiles = c[1];
+  stats.tiles_processed += c[0];
+  stats.bfs_tiles += c[1];
 }
 
 template <typename T>
