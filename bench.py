@@ -437,11 +437,16 @@ def run_serve(args):
     rng = np.random.default_rng(args.seed)
     images = {n: W.tv_image(100 + i, n=n, polygons=30) for i, n in enumerate(SERVE_SIZES)}
     S = lf.LatticeServer(workers=args.workers)
-    # warm-up: every size once per worker (engines and kernels loaded)
-    warm = [S.submit_tv(images[n], 0.01) for n in SERVE_SIZES for _ in range(args.workers)]
-    for t in warm:
-        S.wait(t)
-        S.release(t)
+    # warm-up: every size on every worker (engines built, kernels loaded);
+    # a round of `workers` simultaneous requests spreads over the workers
+    warm = []
+    for _ in range(2):
+        for n in SERVE_SIZES:
+            ts = [S.submit_tv(images[n], 0.01) for _ in range(args.workers)]
+            for t in ts:
+                S.wait(t)
+                S.release(t)
+            warm += ts
     sizes = rng.choice(SERVE_SIZES, size=args.requests)
     lams = np.exp(rng.uniform(np.log(1e-3), np.log(1.0), size=args.requests))
     gaps = rng.exponential(1.0 / args.rate, size=args.requests)

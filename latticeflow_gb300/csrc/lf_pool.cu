@@ -186,14 +186,6 @@ __global__ void k_pool_sum_pos(const InstDesc* insts, const long long* nbase, in
   if (inst >= 0 && sum && (threadIdx.x & 31) == __ffs(peers) - 1) atom_add(&sums[inst], sum);
 }
 
-template <class K>
-int occupancy_grid(K kernel, int threads, size_t smem) {
-  int dev = 0, sms = 1, per = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
-  return std::max(1, per) * sms;
-}
 
 }  // namespace
 

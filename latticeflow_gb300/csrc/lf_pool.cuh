@@ -87,11 +87,10 @@ __device__ __forceinline__ void enqueue_tile(const TileQueue& q, int nxt, int t)
   }
 }
 
-// Block b of a pass works on entry b of the queue; blocks past the number of
-// queued tiles return at once (the grid covers every tile of the pool).
-__device__ __forceinline__ int queued_tile(const TileQueue& q, int cur) {
-  const unsigned n = *((volatile unsigned*)&q.ctr[q_count_idx(cur)]);
-  return blockIdx.x < n ? q.list[cur][blockIdx.x] : -1;
+// Number of tiles queued for the pass reading list `cur` (written by the
+// previous pass); the blocks of a pass stride over the list.
+__device__ __forceinline__ unsigned queued_count(const TileQueue& q, int cur) {
+  return *((volatile unsigned*)&q.ctr[q_count_idx(cur)]);
 }
 #endif  // __CUDACC__
 

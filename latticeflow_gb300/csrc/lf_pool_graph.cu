@@ -7,8 +7,15 @@ cudaError_t launch_pool_bfs(const PoolBFS& p, int KA, int KB, bool single, int g
                                    int threads, size_t smem, cudaStream_t s) {
 #define X(A, B)                                                                 \
   if (KA == A && KB == B) {                                                     \
-    if (single) k_pool_bfs<A, B, true><<<grid, threads, smem, s>>>(p);          \
-    else k_pool_bfs<A, B, false><<<grid, threads, smem, s>>>(p);                \
+    static int cap_t = 0, cap_f = 0;                                            \
+    static size_t cap_smem = 0;                                                 \
+    if (!cap_t || cap_smem != smem) {                                           \
+      cap_t = occupancy_grid(k_pool_bfs<A, B, true>, threads, smem);            \
+      cap_f = occupancy_grid(k_pool_bfs<A, B, false>, threads, smem);           \
+      cap_smem = smem;                                                          \
+    }                                                                           \
+    if (single) k_pool_bfs<A, B, true><<<std::min(grid, cap_t), threads, smem, s>>>(p); \
+    else k_pool_bfs<A, B, false><<<std::min(grid, cap_f), threads, smem, s>>>(p);       \
     return cudaGetLastError();                                                  \
   }
   LF_POOL_PR_LIST(X)
@@ -20,8 +27,15 @@ cudaError_t launch_pool_reach(const PoolReach& p, int KA, int KB, bool single, i
                                      int threads, size_t smem, cudaStream_t s) {
 #define X(A, B)                                                                 \
   if (KA == A && KB == B) {                                                     \
-    if (single) k_pool_reach<A, B, true><<<grid, threads, smem, s>>>(p);        \
-    else k_pool_reach<A, B, false><<<grid, threads, smem, s>>>(p);              \
+    static int cap_t = 0, cap_f = 0;                                            \
+    static size_t cap_smem = 0;                                                 \
+    if (!cap_t || cap_smem != smem) {                                           \
+      cap_t = occupancy_grid(k_pool_reach<A, B, true>, threads, smem);          \
+      cap_f = occupancy_grid(k_pool_reach<A, B, false>, threads, smem);         \
+      cap_smem = smem;                                                          \
+    }                                                                           \
+    if (single) k_pool_reach<A, B, true><<<std::min(grid, cap_t), threads, smem, s>>>(p); \
+    else k_pool_reach<A, B, false><<<std::min(grid, cap_f), threads, smem, s>>>(p);       \
     return cudaGetLastError();                                                  \
   }
   LF_POOL_PR_LIST(X)

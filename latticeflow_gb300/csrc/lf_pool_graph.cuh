@@ -75,23 +75,26 @@ __device__ __forceinline__ void bfs_tile(const PoolBFS& p, const InstDesc& I, Po
 
 template <int KA, int KB, bool SINGLE>
 __global__ void __launch_bounds__(1024, 2) k_pool_bfs(PoolBFS p) {
-  const int gt = queued_tile(p.q, p.cur);
-  if (gt < 0) return;
   extern __shared__ __align__(16) unsigned char smem[];
   PoolSmemHead* hd = reinterpret_cast<PoolSmemHead*>(smem);
   int* s_h = reinterpret_cast<int*>(smem + sizeof(PoolSmemHead));
-  if (!SINGLE) {
-    load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
+  const unsigned n = queued_count(p.q, p.cur);
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x) {
+    const int gt = p.q.list[p.cur][i];
     __syncthreads();
+    if (!SINGLE) {
+      load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
+      __syncthreads();
+    }
+    const InstDesc& I = SINGLE ? p.inst0 : hd->inst;
+    if (threadIdx.x == 0) {
+      p.q.flag[p.cur][gt] = 0;
+      atomicAdd(&p.counters[1], 1ull);
+    }
+    if (I.done) continue;
+    if (I.st.K == KA) bfs_tile<KA>(p, I, hd, s_h, gt);
+    else if (KB != KA && I.st.K == KB) bfs_tile<KB>(p, I, hd, s_h, gt);
   }
-  const InstDesc& I = SINGLE ? p.inst0 : hd->inst;
-  if (threadIdx.x == 0) {
-    p.q.flag[p.cur][gt] = 0;
-    atomicAdd(&p.counters[1], 1ull);
-  }
-  if (I.done) return;
-  if (I.st.K == KA) bfs_tile<KA>(p, I, hd, s_h, gt);
-  else if (KB != KA && I.st.K == KB) bfs_tile<KB>(p, I, hd, s_h, gt);
 }
 
 template <int K>
@@ -162,19 +165,22 @@ __device__ __forceinline__ void reach_tile(const PoolReach& p, const InstDesc& I
 
 template <int KA, int KB, bool SINGLE>
 __global__ void __launch_bounds__(1024, 2) k_pool_reach(PoolReach p) {
-  const int gt = queued_tile(p.q, p.cur);
-  if (gt < 0) return;
   extern __shared__ __align__(16) unsigned char smem[];
   PoolSmemHead* hd = reinterpret_cast<PoolSmemHead*>(smem);
   int* s_mark = reinterpret_cast<int*>(smem + sizeof(PoolSmemHead));
-  if (!SINGLE) {
-    load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
+  const unsigned n = queued_count(p.q, p.cur);
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x) {
+    const int gt = p.q.list[p.cur][i];
     __syncthreads();
+    if (!SINGLE) {
+      load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
+      __syncthreads();
+    }
+    const InstDesc& I = SINGLE ? p.inst0 : hd->inst;
+    if (threadIdx.x == 0) p.q.flag[p.cur][gt] = 0;
+    if (I.st.K == KA) reach_tile<KA>(p, I, s_mark, gt);
+    else if (KB != KA && I.st.K == KB) reach_tile<KB>(p, I, s_mark, gt);
   }
-  const InstDesc& I = SINGLE ? p.inst0 : hd->inst;
-  if (threadIdx.x == 0) p.q.flag[p.cur][gt] = 0;
-  if (I.st.K == KA) reach_tile<KA>(p, I, s_mark, gt);
-  else if (KB != KA && I.st.K == KB) reach_tile<KB>(p, I, s_mark, gt);
 }
 
 }  // namespace lfg

@@ -168,23 +168,26 @@ __device__ void pr_tile(const PoolPR<T>& p, const InstDesc& I, PoolSmemHead* hd,
 // (constant bank); otherwise the tile's descriptor is copied to shared memory.
 template <typename T, int KA, int KB, bool SINGLE>
 __global__ void __launch_bounds__(1024) k_pool_pr(PoolPR<T> p) {
-  const int gt = queued_tile(p.q, p.cur);
-  if (gt < 0) return;
   extern __shared__ __align__(16) unsigned char smem[];
   PoolSmemHead* hd = reinterpret_cast<PoolSmemHead*>(smem);
   unsigned char* sbuf = smem + sizeof(PoolSmemHead);
-  if (!SINGLE) {
-    load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
-    __syncthreads();
+  const unsigned n = queued_count(p.q, p.cur);
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x) {
+    const int gt = p.q.list[p.cur][i];
+    __syncthreads();  // the previous tile is done with shared memory
+    if (!SINGLE) {
+      load_inst(&p.inst[p.tile_inst[gt]], &hd->inst);
+      __syncthreads();
+    }
+    const InstDesc& I = SINGLE ? p.inst0 : hd->inst;
+    if (threadIdx.x == 0) {
+      p.q.flag[p.cur][gt] = 0;
+      atomicAdd(&p.counters[0], 1ull);
+    }
+    if (I.done) continue;
+    if (I.st.K == KA) pr_tile<T, KA>(p, I, hd, sbuf, gt);
+    else if (KB != KA && I.st.K == KB) pr_tile<T, KB>(p, I, hd, sbuf, gt);
   }
-  const InstDesc& I = SINGLE ? p.inst0 : hd->inst;
-  if (threadIdx.x == 0) {
-    p.q.flag[p.cur][gt] = 0;
-    atomicAdd(&p.counters[0], 1ull);
-  }
-  if (I.done) return;
-  if (I.st.K == KA) pr_tile<T, KA>(p, I, hd, sbuf, gt);
-  else if (KB != KA && I.st.K == KB) pr_tile<T, KB>(p, I, hd, sbuf, gt);
 }
 
 }  // namespace lfg
