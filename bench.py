@@ -42,10 +42,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="large_cut",
-                    choices=["large_cut", "plain_cut", "volume_cut", "batch", "serve"])
+                    choices=["large_cut", "plain_cut", "volume_cut", "batch", "serve", "tv_path"])
     ap.add_argument("--requests", type=int, default=200, help="serve: measured requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrivals per second")
     ap.add_argument("--workers", type=int, default=4, help="serve: server workers")
+    ap.add_argument("--max-group", type=int, default=8,
+                    help="serve: largest group of same-shape TV requests solved together")
     ap.add_argument("--batch-size", type=int, default=512)
     ap.add_argument("--no-batch-summary", action="store_true",
                     help="skip the batched-vs-plain summary of the default run")
@@ -436,7 +438,7 @@ def run_serve(args):
     from latticeflow_gb300 import workloads as W
     rng = np.random.default_rng(args.seed)
     images = {n: W.tv_image(100 + i, n=n, polygons=30) for i, n in enumerate(SERVE_SIZES)}
-    S = lf.LatticeServer(workers=args.workers)
+    S = lf.LatticeServer(workers=args.workers, max_group=args.max_group)
     # warm-up: every size on every worker (engines built, kernels loaded);
     # a round of `workers` simultaneous requests spreads over the workers
     warm = []
@@ -484,13 +486,99 @@ def run_serve(args):
         "data": "synthetic (seeded polygon images, latticeflow_gb300/workloads.py)",
         "config": {"workload": "serve", "requests": args.requests, "rate_per_s": args.rate,
                    "sizes": list(SERVE_SIZES), "lambda": "log-uniform [1e-3, 1]",
-                   "kernel": "Full2d_4", "workers": args.workers},
+                   "kernel": "Full2d_4", "workers": args.workers, "max_group": args.max_group},
         "latency_ms": {"p50": round(float(np.percentile(lat_ms, 50)), 2),
                        "p99": round(float(np.percentile(lat_ms, 99)), 2),
                        "max": round(float(lat_ms[-1]), 2)},
-        "per_size": per_size, "max_in_flight": st["max_in_flight"], "clocks": clocks,
+        "per_size": per_size, "max_in_flight": st["max_in_flight"],
+        "grouping": {"max_group": args.max_group, "groups": st["groups"],
+                     "grouped_requests": st["grouped_requests"]},
+        "clocks": clocks,
     }
     if rank == 0:
+        print(json.dumps(out))
+
+
+TV_PATH_N = 1024
+TV_PATH_LAMBDAS = 64
+
+
+def tv_path_lambdas():
+    """64 values 1e-3 * 1000^(i/63): 1e-3 .. 1, log-spaced."""
+    return np.array([1e-3 * 1000.0 ** (i / (TV_PATH_LAMBDAS - 1)) for i in range(TV_PATH_LAMBDAS)])
+
+
+def tv_path_cpu_baseline(f, lams, budget_s=20.0):
+    """Restated reference single-lambda TV on one host core: lambdas taken
+    spread over the path until the budget is spent."""
+    from oracle import oracle as O
+    O.build_port()
+    order = [len(lams) // 2, len(lams) - 1, 0, len(lams) // 4, 3 * len(lams) // 4]
+    secs = []
+    t0 = time.time()
+    for i in order:
+        if secs and time.time() - t0 > budget_s:
+            break
+        _, _, s = O.port_tv_single("Full2d_4", f, float(lams[i]))
+        secs.append(s)
+    return {"value": round(len(secs) / sum(secs), 5), "unit": "lambda solves/s", "cores": 1,
+            "kind": "port",
+            "sample": "%d single-lambda solves of the %dx%d image at lambdas spread over the path "
+                      "(reference parametric flow restated, oracle/lf_oracle.cpp), %.1f s total"
+                      % (len(secs), f.shape[0], f.shape[1], sum(secs))}
+
+
+def run_tv_path(args):
+    """--workload tv_path: the 1024x1024 Full2d_4 TV image at 64 lambdas
+    (calculate2dTVPath, host arrays in and out).  A step is one whole path;
+    value = lambda solves per second."""
+    import torch
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from latticeflow_gb300 import _build
+    _build.build_native()
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    f = W.tv_image(args.seed, n=TV_PATH_N, polygons=30)
+    lams = tv_path_lambdas()
+    for _ in range(args.warmup):
+        lf.calculate2dTVPath(f, lams)
+    if world > 1:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        P = lf.calculate2dTVPath(f, lams)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    if world > 1:
+        t = torch.tensor([wall], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        wall = float(t.item())
+    value = world * args.steps * len(lams) / wall
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": "lambda solves/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * wall / args.steps, 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+        "data": "synthetic (seeded polygon image, latticeflow_gb300/workloads.py)",
+        "config": {"workload": "tv_path", "kernel": "Full2d_4", "shape": [TV_PATH_N, TV_PATH_N],
+                   "lambdas": "64 values 1e-3*1000^(i/63)", "seed": args.seed,
+                   "l2": "inputs larger than L2 (no flush needed)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": round(value, 3), "unit": "lambda solves/s",
+                "h2d_bytes_per_step": int(f.nbytes), "d2h_bytes_per_step": int(P.nbytes),
+                "note": "the step is the public host-array call itself"},
+        "clocks": clocks,
+    }
+    if rank == 0:
+        out["cpu_baseline"] = tv_path_cpu_baseline(f, lams)
         print(json.dumps(out))
 
 
@@ -521,6 +609,10 @@ def _ref_init(workload, seed, batch_size=512):
     if workload == "batch":
         _W["batch"] = make_batch(batch_size, seed=seed)
         return
+    if workload == "tv_path":
+        from latticeflow_gb300 import workloads as W
+        _W["tv"] = (W.tv_image(seed, n=TV_PATH_N, polygons=30), tv_path_lambdas())
+        return
     p = make_workload(workload, seed)
     _W["p"] = p
     _W["e"] = p.energies()
@@ -528,6 +620,10 @@ def _ref_init(workload, seed, batch_size=512):
 
 def _ref_solve(arg):
     from oracle import oracle as O
+    if "tv" in _W:
+        f, lams = _W["tv"]
+        _, _, secs = O.port_tv_single("Full2d_4", f, float(lams[arg % len(lams)]))
+        return secs
     if "batch" in _W:
         secs = 0.0
         for i in arg:
@@ -554,6 +650,11 @@ def run_reference(args):
         p = None
         per_step = args.batch_size
         work = [list(range(c, args.batch_size, cores)) for c in range(cores)]
+    elif args.workload == "tv_path":
+        p = None
+        per_step = cores
+        # lambdas spread over the path, one per core
+        work = [(c * TV_PATH_LAMBDAS) // cores for c in range(cores)]
     else:
         p = make_workload(args.workload, args.seed)
         per_step = cores
@@ -568,21 +669,29 @@ def run_reference(args):
         wall = time.time() - t0
     value = per_step * args.steps / wall
     kind = "port"
+    unit = "lambda solves/s" if args.workload == "tv_path" else UNIT
     out = {
-        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": unit,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * wall / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int64",
         "data": "synthetic (seeded generator, latticeflow_gb300/workloads.py)",
-        "config": workload_config(args.workload, p) if p is not None else
-                  {"workload": "batch", "lattices": args.batch_size},
-        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": kind,
+        "config": (workload_config(args.workload, p) if p is not None else
+                   {"workload": "batch", "lattices": args.batch_size}
+                   if args.workload == "batch" else
+                   {"workload": "tv_path", "kernel": "Full2d_4", "shape": [TV_PATH_N, TV_PATH_N],
+                    "lambdas": "64 values 1e-3*1000^(i/63)", "seed": args.seed}),
+        "cpu_baseline": {"value": round(value, 4), "unit": unit, "cores": cores, "kind": kind,
                          "sample": ("each step: one full solve per host core in parallel"
+                                    " (reference push-relabel restated, oracle/lf_oracle.cpp)"
                                     if p is not None else
                                     "each step: all %d lattices spread over the host cores"
-                                    % args.batch_size) +
-                                   " (reference push-relabel restated, oracle/lf_oracle.cpp)"},
-        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                                    " (reference push-relabel restated, oracle/lf_oracle.cpp)"
+                                    % args.batch_size if args.workload == "batch" else
+                                    "each step: one single-lambda TV solve per host core, lambdas "
+                                    "spread over the path (reference parametric flow restated, "
+                                    "oracle/lf_oracle.cpp)")},
+        "e2e": {"value": round(value, 4), "unit": unit, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -596,6 +705,8 @@ def main():
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "tv_path":
+        run_tv_path(args)
     else:
         run_ours(args)
 

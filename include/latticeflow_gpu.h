@@ -149,7 +149,9 @@ int lf_get_stream(const lf_lattice* h, void** stream_out);
  * per global relabel); 0 keeps the current/auto value. */
 int lf_set_tuning(lf_lattice* h, int tile_rows, int local_sweeps, int launches_per_relabel);
 /* One knob by name: "tile_rows", "local_sweeps", "launches_per_relabel",
- * "height_slack", "pass_chunk".  LF_ERR_INVALID for an unknown name. */
+ * "height_slack", "pass_chunk", "tail_active" (at most this many active
+ * nodes switch an epoch to routing their excess along BFS trees; 0 = 64,
+ * negative = never).  LF_ERR_INVALID for an unknown name. */
 int lf_set_param(lf_lattice* h, const char* name, int value);
 
 /* -------------------------------------------------------------- batches
@@ -186,7 +188,10 @@ int lf_batch_get_stats(const lf_batch* b, int64_t* epochs, int64_t* pr_passes, i
  * HBM budget still free (budget 0 = half the free device memory; a request
  * larger than the budget runs alone).  Admitted requests run concurrently
  * on the workers' own CUDA streams, so their kernels overlap on the device;
- * each worker keeps the engines of the shapes it has served.  Inputs are
+ * each worker keeps the engines of the shapes it has served.  TV requests
+ * of one kernel and shape that wait together are solved as one stacked
+ * problem (continuous batching, groups of 1, 2, 4, ... up to max_group,
+ * default 8); each result equals the request's own solve.  Inputs are
  * copied at submission; results stay until lf_server_release.  Latency =
  * completion - submission (queueing included). */
 typedef struct lf_server lf_server;
@@ -205,6 +210,10 @@ int lf_server_get_cut(lf_server* s, int64_t ticket, int* cut, int64_t* flow, int
 int lf_server_release(lf_server* s, int64_t ticket);
 int lf_server_stats(lf_server* s, double* p50_ms, double* p99_ms, double* solves_per_s,
                     int64_t* completed, int64_t* max_in_flight);
+/* max_group = 1 turns grouping off. */
+int lf_server_set_max_group(lf_server* s, int max_group);
+/* groups: stacked solves run so far; grouped: requests they held. */
+int lf_server_group_stats(lf_server* s, int64_t* groups, int64_t* grouped);
 
 /* ------------------------------------------------------ no allocation
  * No counterpart in the reference.  A binary cut of one small 2-d lattice
@@ -234,6 +243,27 @@ int lf_cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* s
  * levels_out (may be NULL): the final 2x-scaled fixed-point values r. */
 int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double lambda,
              double* out, int64_t* levels_out);
+
+/* calculate2dTV<Kernel, int64>(nx, ny, f, vector<double> lambdas)
+ * (tv/tv_solver.hpp:657-681): the denoised image at every lambda,
+ * out[n_lambda][nx][ny].  Slice i is the single-lambda solution at
+ * lambdas[i] (what lf_tv_2d returns), all lambdas solved together.  The
+ * reference traces the path instead with piecewise-linear region segments
+ * (tv/tv_regpath_node.hpp), whose values differ from its own single-lambda
+ * solutions away from the smallest lambdas.  As in the reference a negative
+ * lambda counts as 0 and n_lambda = 0 returns at once. */
+int lf_tv_2d_path(const char* kernel, size_t nx, size_t ny, const double* f, size_t n_lambda,
+                  const double* lambdas, double* out);
+
+/* Many single-lambda TV problems of one shape solved together on the GPU:
+ * problem p is the image at f + p * f_stride (f_stride = 0: one image for
+ * all problems) at lambda lambdas[p]; out (and levels_out, may be NULL) hold
+ * count * nx * ny values, problem-major.  max_nodes bounds the lattice nodes
+ * of one stacked solve (0 = 2^26); larger batches run as several stacks.
+ * No reference counterpart (the reference solves one image per call). */
+int lf_tv_2d_batch(const char* kernel, size_t nx, size_t ny, size_t count, const double* f,
+                   size_t f_stride, const double* lambdas, double* out, int64_t* levels_out,
+                   size_t max_nodes);
 
 #ifdef __cplusplus
 }

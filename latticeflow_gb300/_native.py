@@ -46,6 +46,8 @@ PROTOTYPES = {
     "lf_get_stream": (I, [P, P]),
     "lf_get_layout": (I, [P, P, P, P]),
     "lf_tv_2d": (I, [ctypes.c_char_p, SZ, SZ, P, ctypes.c_double, P, P]),
+    "lf_tv_2d_path": (I, [ctypes.c_char_p, SZ, SZ, P, SZ, P, P]),
+    "lf_tv_2d_batch": (I, [ctypes.c_char_p, SZ, SZ, SZ, P, SZ, P, P, P, SZ]),
     "lf_batch_create": (I, [P]),
     "lf_batch_destroy": (None, [P]),
     "lf_batch_add": (I, [P, ctypes.c_char_p, I, P, P]),
@@ -70,6 +72,8 @@ PROTOTYPES = {
     "lf_server_get_cut": (I, [P, ctypes.c_int64, P, P, P]),
     "lf_server_release": (I, [P, ctypes.c_int64]),
     "lf_server_stats": (I, [P, P, P, P, P, P]),
+    "lf_server_set_max_group": (I, [P, I]),
+    "lf_server_group_stats": (I, [P, P, P]),
 }
 
 LF_OK = 0

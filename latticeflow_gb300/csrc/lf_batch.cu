@@ -201,6 +201,7 @@ void Batch::run() {
       I.st = members[i].st;
       I.node_base = members[i].node_base;
       I.res_base = members[i].res_base;
+      I.plane = members[i].g.NP;
       I.tile_base = members[i].tile_base;
       I.hmax = kHInf - 2;
       I.active = 1;

@@ -3,6 +3,7 @@
 #include <exception>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/latticeflow_gpu.h"
 #include "lf_batch.h"
@@ -238,6 +239,7 @@ int lf_set_param(lf_lattice* h, const char* name, int value) {
     else if (n == "launches_per_relabel") t.launches_per_relabel = value;
     else if (n == "height_slack") t.height_slack = value;
     else if (n == "pass_chunk") t.pass_chunk = value;
+    else if (n == "tail_active") t.tail_active = value;
     else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
   });
 }
@@ -279,17 +281,50 @@ int lf_get_stream(const lf_lattice* h, void** out) {
   return LF_OK;
 }
 
+namespace {
+const lfg::KernelDef* tv_kernel(const char* kernel) {
+  const lfg::KernelDef* k = kernel ? lfg::find_kernel(kernel) : nullptr;
+  if (!k) throw lfg::LfError{LF_ERR_BAD_NAME, std::string("Bad Kernel or Solver Name: ") +
+                                                  (kernel ? kernel : "(null)")};
+  if (k->nd != 2 || !k->geocut)
+    throw lfg::LfError{LF_ERR_BAD_NAME, "Kernel is not valid for GeoCuts or TV Minimization."};
+  return k;
+}
+}  // namespace
+
 int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double lambda,
              double* out, int64_t* levels_out) {
   return guarded([&] {
-    const lfg::KernelDef* k = kernel ? lfg::find_kernel(kernel) : nullptr;
-    if (!k) throw lfg::LfError{LF_ERR_BAD_NAME, std::string("Bad Kernel or Solver Name: ") +
-                                                    (kernel ? kernel : "(null)")};
-    if (k->nd != 2 || !k->geocut)
-      throw lfg::LfError{LF_ERR_BAD_NAME, "Kernel is not valid for GeoCuts or TV Minimization."};
+    const lfg::KernelDef* k = tv_kernel(kernel);
     if (!f || !out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
     int rc = lfg::tv_2d(k, nx, ny, f, lambda, out, levels_out);
     if (rc) throw lfg::LfError{rc, "tv solve failed"};
+  });
+}
+
+int lf_tv_2d_path(const char* kernel, size_t nx, size_t ny, const double* f, size_t n_lambda,
+                  const double* lambdas, double* out) {
+  return guarded([&] {
+    const lfg::KernelDef* k = tv_kernel(kernel);
+    if (n_lambda == 0 || nx * ny == 0) return;
+    if (!f || !out || !lambdas) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    std::vector<double> lam(lambdas, lambdas + n_lambda);
+    for (double& l : lam)
+      if (!(l >= 0)) l = 0;  // tv_solver.hpp:669-674
+    int rc = lfg::tv_2d_batch(k, nx, ny, n_lambda, f, 0, lam.data(), out, nullptr, 0);
+    if (rc) throw lfg::LfError{rc, "tv path failed"};
+  });
+}
+
+int lf_tv_2d_batch(const char* kernel, size_t nx, size_t ny, size_t count, const double* f,
+                   size_t f_stride, const double* lambdas, double* out, int64_t* levels_out,
+                   size_t max_nodes) {
+  return guarded([&] {
+    const lfg::KernelDef* k = tv_kernel(kernel);
+    if (count == 0 || nx * ny == 0) return;
+    if (!f || !out || !lambdas) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    int rc = lfg::tv_2d_batch(k, nx, ny, count, f, f_stride, lambdas, out, levels_out, max_nodes);
+    if (rc) throw lfg::LfError{rc, "tv batch failed"};
   });
 }
 
@@ -379,6 +414,24 @@ int lf_server_stats(lf_server* s, double* p50, double* p99, double* sps, int64_t
     s->s->stats(p50, p99, sps, &c, &m);
     if (completed) *completed = c;
     if (max_in_flight) *max_in_flight = m;
+  });
+}
+
+int lf_server_set_max_group(lf_server* s, int max_group) {
+  return guarded([&] {
+    if (!s) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    if (max_group < 1) throw lfg::LfError{LF_ERR_INVALID, "max_group must be at least 1"};
+    s->s->set_max_group(max_group);
+  });
+}
+
+int lf_server_group_stats(lf_server* s, int64_t* groups, int64_t* grouped) {
+  return guarded([&] {
+    if (!s) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    long long a = 0, b = 0;
+    s->s->group_stats(&a, &b);
+    if (groups) *groups = a;
+    if (grouped) *grouped = b;
   });
 }
 
@@ -494,6 +547,7 @@ int lf_batch_set_param(lf_batch* b, const char* name, int value) {
     else if (n == "launches_per_relabel") t.launches_per_relabel = value;
     else if (n == "height_slack") t.height_slack = value;
     else if (n == "pass_chunk") t.pass_chunk = value;
+    else if (n == "tail_active") t.tail_active = value;
     else if (n == "defer_checks") b->b->defer_checks = value != 0;
     else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
   });

@@ -244,12 +244,40 @@ void Engine::prepare_working(int elem) {
     check(cudaMalloc(&d_mark, g.NP * sizeof(int)), "cudaMalloc mark");
   }
   if (!runner_ready) {
-    InstDesc I{};
-    I.g = g;
-    I.st = st;
-    I.hmax = kHInf - 2;
-    I.active = 1;
-    runner.setup(std::vector<InstDesc>(1, I), stream);
+    std::vector<InstDesc> insts;
+    if (sub_count <= 1) {
+      InstDesc I{};
+      I.g = g;
+      I.st = st;
+      I.plane = g.NP;
+      I.hmax = kHInf - 2;
+      I.active = 1;
+      insts.push_back(I);
+    } else {
+      // sub_count lattices of sub_real_rows real rows stacked along the
+      // second axis every sub_rows rows: one pool instance each (own epoch
+      // height cap, own finish), sharing this lattice's residual planes
+      if (nd != 2 || g.Bp != (long long)sub_rows * sub_count || sub_rows % 32)
+        throw LfError{2, "stacked lattices do not tile the padded rows"};
+      size_t sd[2] = {(size_t)sub_real_rows, dims[1]};
+      Geo gs{};
+      lattice_geometry(2, sd, st, elem, tune.tile_rows, gs);
+      if (gs.Bp != sub_rows || gs.Cp != g.Cp || gs.TB != g.TB || gs.TC != g.TC)
+        throw LfError{2, "stacked lattice geometry mismatch"};
+      for (int c = 0; c < sub_count; ++c) {
+        InstDesc I{};
+        I.g = gs;
+        I.st = st;
+        I.node_base = (long long)c * gs.NP;
+        I.res_base = (long long)c * gs.NP;
+        I.plane = g.NP;
+        I.tile_base = c * gs.ntiles;
+        I.hmax = kHInf - 2;
+        I.active = 1;
+        insts.push_back(I);
+      }
+    }
+    runner.setup(insts, stream);
     runner_ready = true;
   }
   if (elem == 4) {

@@ -83,6 +83,10 @@ class Engine : public ProfHooks {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   PoolRunner runner;
   bool runner_ready = false;
+  // > 1: the lattice holds sub_count independent lattices of sub_real_rows
+  // rows each, stacked every sub_rows (a multiple of 32) rows; each is its
+  // own pool instance in the solve
+  int sub_count = 1, sub_rows = 0, sub_real_rows = 0;
   // profiling: event pairs around launches, summed per category after run()
   std::vector<cudaEvent_t> pev;
   std::vector<int> pcat;
@@ -106,11 +110,19 @@ class Engine : public ProfHooks {
 };
 
 void engine_run_parametric(Engine& E);  // lf_param.cu
+// engine of `count` stacked nx x ny TV problems (count 1: a plain lattice)
+Engine* new_tv_stack_engine(const KernelDef* kd, size_t nx, size_t ny, size_t count);
 int cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* src,
                    const int32_t* snk, const int32_t* edge, int32_t* cut, int64_t* flow_energy,
                    cudaStream_t s);  // lf_noalloc.cu
 int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lambda, double* out,
           int64_t* levels_out);
 int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* levels_out);
+int tv_2d_stack_on(Engine& E, size_t nx, size_t ny, size_t count, const double* f,
+                   size_t f_stride, const double* lambdas, double* out, int64_t* levels_out);
+size_t tv_stack_size(size_t nx, size_t ny, size_t count, size_t max_nodes);
+int tv_2d_batch(const KernelDef* kd, size_t nx, size_t ny, size_t count, const double* f,
+                size_t f_stride, const double* lambdas, double* out, int64_t* levels_out,
+                size_t max_nodes);
 
 }  // namespace lfg

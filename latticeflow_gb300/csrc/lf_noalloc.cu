@@ -148,6 +148,7 @@ int cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* src,
   InstDesc I{};
   I.g = g;
   I.st = st;
+  I.plane = g.NP;
   I.hmax = kHInf - 2;
   I.active = 1;
   const long long nb[2] = {0, g.NP};

@@ -23,7 +23,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <climits>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "lf_engine.h"
@@ -71,27 +73,37 @@ __global__ void k_fill_energy_pf(Geo g, Stencil st, int nd, long long N, const i
 
 // TV setup (tv/tv_solver.hpp:71-112): node value uf (fixed point) enters as
 // reduction 2 uf; every in-lattice edge of direction k gets 2 pwf[k].
-__global__ void k_fill_tv(Geo g, Stencil st, int nd, long long N, const int64_t* uf,
-                          const long long* pwf2, long long* exc, long long* cap) {
+// Several problems of one shape may be stacked along the rows: problem p holds
+// `nx` real rows starting at row p*rows, its values at uf + p*uf_stride
+// (uf_stride 0: one image shared by all problems) and its edge weights at
+// pwf2 + p*K; edges leaving a problem get no capacity.  N = problems*nx*C.
+__global__ void k_fill_tv(Geo g, Stencil st, long long N, int nx, int rows, long long uf_stride,
+                          const int64_t* uf, const long long* pwf2, long long* exc,
+                          long long* cap) {
   long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= N) return;
-  int a, bb, c;
-  bounded_coords(g, nd, b, a, bb, c);
-  long long u = ((long long)a * g.Bp + bb) * g.Cp + c;
-  exc[u] = -2LL * uf[b];
+  const long long per = (long long)nx * g.C;
+  const int p = int(b / per);
+  const long long q = b - p * per;
+  const int lo = p * rows, hi = lo + nx;
+  const int bb = lo + int(q / g.C), c = int(q % g.C);
+  long long u = (long long)bb * g.Cp + c;
+  exc[u] = -2LL * uf[p * uf_stride + q];
   for (int k = 0; k < st.K; ++k) {
-    int na = a + st.da[k], nb = bb + st.db[k], nc = c + st.dc[k];
-    bool in = na >= 0 && na < g.A && nb >= 0 && nb < g.B && nc >= 0 && nc < g.C;
-    cap[(long long)k * g.NP + u] = in ? pwf2[k] : 0;
+    int nb = bb + st.db[k], nc = c + st.dc[k];
+    bool in = st.da[k] == 0 && nb >= lo && nb < hi && nc >= 0 && nc < g.C;
+    cap[(long long)k * g.NP + u] = in ? pwf2[(long long)p * st.K + k] : 0;
   }
 }
 
-// Section of every in-lattice node = 0, padding = -1.
-__global__ void k_pf_init_keys(Geo g, int* key) {
+// Section of every in-lattice node = its problem's index (problems every
+// `rows` rows along the second axis, the first `real` of them in the
+// lattice), padding = -1.
+__global__ void k_pf_init_keys(Geo g, int rows, int real, int* key) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.NP) return;
   int c = int(i % g.Cp), b = int((i / g.Cp) % g.Bp), a = int(i / ((long long)g.Cp * g.Bp));
-  key[i] = (a < g.A && b < g.B && c < g.C) ? 0 : -1;
+  key[i] = (a < g.A && b < g.B && c < g.C && b % rows < real) ? b / rows : -1;
 }
 
 // Per-section r statistics: 128-bit sum (lo, hi), count, min, max.
@@ -222,7 +234,8 @@ cudaError_t launch_fill_energy_pf(const Geo& g, const Stencil& st, int nd, long 
 }
 
 // The parametric driver over an engine whose accumulators hold the 2x-scaled
-// reductions (exc64 = -reduction) and alphas (cap64).
+// reductions (exc64 = -reduction) and alphas (cap64).  An engine holding
+// stacked lattices (sub_count > 1) starts with one section per lattice.
 void engine_run_parametric(Engine& E) {
   // Section solves move small excess over long distances through
   // high-capacity regions: more local sweeps per tile visit and more passes
@@ -230,6 +243,11 @@ void engine_run_parametric(Engine& E) {
   // problems: 6.7x fewer milliseconds at 1024^2 than the binary-cut setting).
   if (E.tune.sweeps <= 0) E.tune.sweeps = 16;
   if (E.tune.launches_per_relabel <= 0) E.tune.launches_per_relabel = 64;
+  // The tail step (BFS trees from the last active nodes) pays for binary
+  // cuts; section solves leave small deficits spread over large sections,
+  // so its trees span whole sections and cost more than the passes they save
+  // (measured at 1024^2: 1.45 s -> 3.3 s for lambda = 0.05).
+  if (E.tune.tail_active == 0) E.tune.tail_active = -1;
   E.alloc_accumulators();
   E.stats = SolveStats();
   E.prepare_working(8);
@@ -237,7 +255,10 @@ void engine_run_parametric(Engine& E) {
   cudaStream_t s = E.stream;
   long long* exc = (long long*)E.d_exc;
   const long long NP = g.NP;
-  const long long cap_sections = std::max<long long>(E.N, 1) + 1;
+  const int problems = std::max(E.sub_count, 1);
+  const int rows = problems > 1 ? E.sub_rows : std::max(E.g.B, 1);
+  const int real = problems > 1 ? E.sub_real_rows : rows;
+  const long long cap_sections = std::max<long long>(E.N, 1) + problems;
 
   DevBuf<int> key;
   DevBuf<long long> off_old, off_new, rmin, rmax;
@@ -259,16 +280,16 @@ void engine_run_parametric(Engine& E) {
   // (the section mask stays allocated with the engine for its next solve)
 
   E.check(cudaEventRecord(E.ev0, s), "event");
-  k_pf_init_keys<<<nblk(NP, 256), 256, 0, s>>>(g, key.p);
+  k_pf_init_keys<<<nblk(NP, 256), 256, 0, s>>>(g, rows, real, key.p);
   E.check(E.counted(cudaGetLastError()), "init keys");
-  E.check(cudaMemsetAsync(off_old.p, 0, sizeof(long long), s), "memset");
+  E.check(cudaMemsetAsync(off_old.p, 0, problems * sizeof(long long), s), "memset");
 
-  long long S = E.N > 0 ? 1 : 0;  // sections of the current generation, ids 0..S-1
+  long long S = E.N > 0 ? problems : 0;  // sections of the current generation, ids 0..S-1
   std::vector<unsigned long long> h_lo, h_hi, h_cnt, h_cnt2;
   std::vector<long long> h_min, h_max, h_off, h_new;
   std::vector<unsigned char> h_fin;
   std::vector<int> h_child;
-  const long long max_rounds = 100000;
+  const long long max_rounds = 20000;
   const bool trace = std::getenv("LF_PF_TRACE") != nullptr;  // diagnostic: one line per generation
   for (long long round = 0; S > 0; ++round) {
     const auto tr0 = std::chrono::steady_clock::now();
@@ -300,6 +321,12 @@ void engine_run_parametric(Engine& E) {
       double count = double(h_cnt[i]);
       long long r_new = (long long)std::ceil(double(sum) / count);
       if (r_new == h_max[i]) --r_new;
+      // The double quotient rounds to r_min when the mean exceeds r_min by
+      // less than its resolution (sections of more than ~2^12 nodes at
+      // 41-bit values); no node then holds excess, nothing moves, and the
+      // reference requeues the same range for ever.  The exact ceiling is
+      // then r_min + 1 (the mean is above r_min whenever r_max > r_min).
+      if (r_new <= h_min[i]) r_new = h_min[i] + 1;
       h_new[i] = r_new;
       ++solving;
     }
@@ -362,58 +389,114 @@ void engine_run_parametric(Engine& E) {
   E.solved = true;
 }
 
-// calculate2dTV<Kernel, int64>(nx, ny, f, lambda)  (tv/tv_solver.hpp:650-655)
-// on an existing parametric engine of shape (nx, ny) (its buffers are reused).
-int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* levels_out) {
-  const KernelDef* kd = E.kd;
-  const size_t nx = E.dims[0], ny = E.dims[1];
-  const int nbits = 40;  // n_bits_function_precision for int64 (pf_flow_node.hpp:103-115)
-  const double fscale = double(int64_t(1) << nbits);
-  const size_t N = nx * ny;
-  if (N == 0) return 0;
-  // setup (tv_solver.hpp:71-112), sequential double arithmetic as the reference
+namespace {
+
+// TV setup of one image (tv/tv_solver.hpp:71-112), sequential double
+// arithmetic as the reference: mean, scale = 2 max |f - mean|, node values in
+// 40-bit fixed point (n_bits_function_precision for int64,
+// pf_flow_node.hpp:103-115).
+struct TVImage {
+  double mean = 0, scale = 0;
+  std::vector<int64_t> uf;
+};
+constexpr int kTVBits = 40;
+
+TVImage tv_setup(const double* f, size_t N) {
+  TVImage t;
+  const double fscale = double(int64_t(1) << kTVBits);
   double v_min = f[0], v_max = f[0], v_sum = f[0];
   for (size_t i = 1; i < N; ++i) {
     v_min = std::min(v_min, f[i]);
     v_max = std::max(v_max, f[i]);
     v_sum += f[i];
   }
-  const double mean = v_sum / double(N);
-  v_min -= mean;
-  v_max -= mean;
-  const double scale = 2 * std::max(v_max, -v_min);
-  const double max_lambda = std::max(lambda, 1e-8);
-  std::vector<int64_t> uf(N);
-  for (size_t i = 0; i < N; ++i) uf[i] = int64_t(std::round((0.5 + (f[i] - mean) / scale) * fscale));
-  const double gsv = 0.5 / (scale * max_lambda);
-  std::vector<long long> pwf2(kd->K);
+  t.mean = v_sum / double(N);
+  v_min -= t.mean;
+  v_max -= t.mean;
+  t.scale = 2 * std::max(v_max, -v_min);
+  t.uf.resize(N);
+  for (size_t i = 0; i < N; ++i)
+    t.uf[i] = int64_t(std::round((0.5 + (f[i] - t.mean) / t.scale) * fscale));
+  return t;
+}
+
+// Edge values 2 pwf[k] for one lambda (tv_solver.hpp:90-110, max_lambda = lambda).
+void tv_edges(const KernelDef* kd, double scale, double lambda, long long* pwf2) {
+  const double fscale = double(int64_t(1) << kTVBits);
+  const double gsv = 0.5 / (scale * std::max(lambda, 1e-8));
   for (int k = 0; k < kd->K; ++k)
     pwf2[k] = 2LL * (long long)std::round((gsv * kd->weight[k]) / scale * fscale);
+}
+
+}  // namespace
+
+// `count` single-lambda TV problems of one shape nx x ny solved together on
+// an engine of shape (count * nx, ny): problem p is image f + p * f_stride
+// (f_stride 0: every problem uses the same image) at lambdas[p]
+// (calculate2dTV<Kernel, int64>(nx, ny, f, lambda), tv/tv_solver.hpp:650-655,
+// once per problem).  The problems never share a section, so each one's
+// levels equal its own single solve.
+int tv_2d_stack_on(Engine& E, size_t nx, size_t ny, size_t count, const double* f,
+                   size_t f_stride, const double* lambdas, double* out, int64_t* levels_out) {
+  const KernelDef* kd = E.kd;
+  const size_t N = nx * ny;
+  if (N == 0 || count == 0) return 0;
+  const size_t rows = count > 1 ? size_t(E.sub_rows) : nx;
+  if (E.nd != 2 || E.dims[1] != ny || (count > 1 && (size_t(E.sub_count) != count ||
+                                                     size_t(E.sub_real_rows) != nx)) ||
+      (count == 1 && (E.sub_count > 1 || E.dims[0] != nx)))
+    throw LfError{2, "engine shape does not match the stacked problems"};
+  const double fscale = double(int64_t(1) << kTVBits);
+  const size_t n_images = f_stride ? count : 1;
+  std::vector<TVImage> img(n_images);
+  for (size_t p = 0; p < n_images; ++p) img[p] = tv_setup(f + p * f_stride, N);
+  std::vector<long long> pwf2(count * kd->K);
+  for (size_t p = 0; p < count; ++p)
+    tv_edges(kd, img[f_stride ? p : 0].scale, lambdas[p], &pwf2[p * kd->K]);
 
   E.alloc_accumulators();
   DevBuf<int64_t> d_uf;
   DevBuf<long long> d_pwf;
-  d_uf.alloc(N, E.stream);
-  d_pwf.alloc(kd->K, E.stream);
-  E.check(cudaMemcpyAsync(d_uf.p, uf.data(), N * 8, cudaMemcpyHostToDevice, E.stream), "memcpy");
-  E.check(cudaMemcpyAsync(d_pwf.p, pwf2.data(), kd->K * 8, cudaMemcpyHostToDevice, E.stream), "memcpy");
-  k_fill_tv<<<nblk((long long)N, 256), 256, 0, E.stream>>>(E.g, E.st, 2, (long long)N, d_uf.p,
-                                                           d_pwf.p, E.d_exc64, E.d_cap64);
+  d_uf.alloc(n_images * N, E.stream);
+  d_pwf.alloc(pwf2.size(), E.stream);
+  for (size_t p = 0; p < n_images; ++p)
+    E.check(cudaMemcpyAsync(d_uf.p + p * N, img[p].uf.data(), N * 8, cudaMemcpyHostToDevice,
+                            E.stream), "memcpy");
+  E.check(cudaMemcpyAsync(d_pwf.p, pwf2.data(), pwf2.size() * 8, cudaMemcpyHostToDevice,
+                          E.stream), "memcpy");
+  const long long NT = (long long)(N * count);
+  k_fill_tv<<<nblk(NT, 256), 256, 0, E.stream>>>(E.g, E.st, NT, int(nx), int(rows),
+                                                  f_stride ? (long long)N : 0LL, d_uf.p, d_pwf.p,
+                                                  E.d_exc64, E.d_cap64);
   E.check(cudaGetLastError(), "fill tv");
+  // the image values are no longer needed once filled
+  for (auto& t : img) std::vector<int64_t>().swap(t.uf);
   engine_run_parametric(E);
   // output (tv_solver.hpp:159-175): value of r/2 in the fixed point, mean removed
   std::vector<double> R(N);
-  double sum = 0;
-  for (size_t i = 0; i < N; ++i) {
-    int64_t r = E.levels_host[i];
-    if (levels_out) levels_out[i] = r;
-    double x = double(r / 2) / fscale;
-    double v = (x - 0.5) * scale + mean;
-    R[i] = v;
-    sum += v;
+  for (size_t p = 0; p < count; ++p) {
+    const TVImage& t = img[f_stride ? p : 0];
+    // levels_host: the engine's logical rows, problem p from row p * rows
+    const int64_t* lv = E.levels_host.data() + p * rows * ny;
+    double sum = 0;
+    for (size_t i = 0; i < N; ++i) {
+      int64_t r = lv[i];
+      if (levels_out) levels_out[p * N + i] = r;
+      double x = double(r / 2) / fscale;
+      double v = (x - 0.5) * t.scale + t.mean;
+      R[i] = v;
+      sum += v;
+    }
+    double* o = out + p * N;
+    for (size_t i = 0; i < N; ++i) o[i] = (R[i] - sum / double(N)) * t.scale + t.mean;
   }
-  for (size_t i = 0; i < N; ++i) out[i] = (R[i] - sum / double(N)) * scale + mean;
   return 0;
+}
+
+// calculate2dTV<Kernel, int64>(nx, ny, f, lambda)  (tv/tv_solver.hpp:650-655)
+// on an existing parametric engine of shape (nx, ny) (its buffers are reused).
+int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* levels_out) {
+  return tv_2d_stack_on(E, E.dims[0], E.dims[1], 1, f, 0, &lambda, out, levels_out);
 }
 
 int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lambda, double* out,
@@ -422,6 +505,55 @@ int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lam
   size_t dims[2] = {nx, ny};
   Engine E("GPULevelReductions", kd, 2, dims);
   return tv_2d_on(E, f, lambda, out, levels_out);
+}
+
+Engine* new_tv_stack_engine(const KernelDef* kd, size_t nx, size_t ny, size_t count) {
+  if (count <= 1) {
+    size_t dims[2] = {nx, ny};
+    return new Engine("GPULevelReductions", kd, 2, dims);
+  }
+  const size_t rows = (nx + 31) / 32 * 32;  // the padded rows of one lattice
+  if (rows * count > size_t(INT_MAX / 2)) throw LfError{2, "stack too tall"};
+  size_t dims[2] = {rows * count, ny};
+  Engine* E = new Engine("GPULevelReductions", kd, 2, dims);
+  E->sub_count = int(count);
+  E->sub_rows = int(rows);
+  E->sub_real_rows = int(nx);
+  return E;
+}
+
+// Problems per stacked solve: as many as keep the stack within max_nodes.
+size_t tv_stack_size(size_t nx, size_t ny, size_t count, size_t max_nodes) {
+  const size_t N = std::max<size_t>(nx * ny, 1);
+  size_t per = std::max<size_t>(max_nodes / N, 1);
+  per = std::min(per, count);
+  // INT_MAX / 2 rows at most in one engine
+  per = std::min(per, std::max<size_t>(size_t(INT_MAX / 2) / ((nx + 31) / 32 * 32), 1));
+  return std::max<size_t>(per, 1);
+}
+
+// Many single-lambda TV problems of one shape, in stacks of at most
+// max_nodes lattice nodes (0: 2^26).
+int tv_2d_batch(const KernelDef* kd, size_t nx, size_t ny, size_t count, const double* f,
+                size_t f_stride, const double* lambdas, double* out, int64_t* levels_out,
+                size_t max_nodes) {
+  const size_t N = nx * ny;
+  if (N == 0 || count == 0) return 0;
+  if (max_nodes == 0) max_nodes = size_t(1) << 26;
+  const size_t per = tv_stack_size(nx, ny, count, max_nodes);
+  std::unique_ptr<Engine> E;
+  size_t E_count = 0;
+  for (size_t p0 = 0; p0 < count; p0 += per) {
+    const size_t m = std::min(per, count - p0);
+    if (!E || E_count != m) {
+      E.reset();
+      E.reset(new_tv_stack_engine(kd, nx, ny, m));
+      E_count = m;
+    }
+    tv_2d_stack_on(*E, nx, ny, m, f + p0 * f_stride, f_stride, lambdas + p0, out + p0 * N,
+                   levels_out ? levels_out + p0 * N : nullptr);
+  }
+  return 0;
 }
 
 }  // namespace lfg

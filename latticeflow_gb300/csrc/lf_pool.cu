@@ -16,6 +16,8 @@
 #include <algorithm>
 #include <chrono>
 #include <climits>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "lf_pool_runner.h"
@@ -78,7 +80,7 @@ __global__ void k_pool_mask(const InstDesc* insts, const long long* nbase, int n
   const T* r = res + I.res_base;
   uint64_t m = 0;
   for (int k = 0; k < I.st.K; ++k)
-    if (r[(long long)k * I.g.NP + li] > 0) m |= 1ull << k;
+    if (r[(long long)k * I.plane + li] > 0) m |= 1ull << k;
   if (kmask) m &= kmask[i];
   mask[i] = m;
 }
@@ -279,6 +281,42 @@ void PoolRunner::release() {
   cudaFree(d_flag); d_flag = nullptr;
   cudaFree(d_counters); d_counters = nullptr;
   if (h_pin) { cudaFreeHost(h_pin); h_pin = nullptr; }
+  free_tail();
+}
+
+void PoolRunner::free_tail() {
+  cudaFree(tail.vis);
+  cudaFree(tail.node);
+  cudaFree(tail.par);
+  cudaFree(tail.dir);
+  cudaFree(tail.dem);
+  cudaFree(tail.rem);
+  cudaFree(tail.lvl);
+  cudaFree(tail.list);
+  cudaFree(tail.count);
+  tail = TailScratch();
+  tail_stamp = 1;
+}
+
+// Tail scratch, allocated at the first tail step of this pool.
+void PoolRunner::alloc_tail() {
+  if (tail.vis) return;
+  TailScratch t;
+  t.cap = int(std::min<long long>(std::max<long long>(NP, 1), 1LL << 22));
+  t.lvl_cap = 1 << 16;
+  t.max_active = 64;
+  check(cudaMalloc(&t.vis, std::max<long long>(NP, 1) * sizeof(int)), "cudaMalloc tail");
+  check(cudaMalloc(&t.node, t.cap * sizeof(long long)), "cudaMalloc tail");
+  check(cudaMalloc(&t.par, t.cap * sizeof(int)), "cudaMalloc tail");
+  check(cudaMalloc(&t.dir, t.cap), "cudaMalloc tail");
+  check(cudaMalloc(&t.dem, t.cap * sizeof(long long)), "cudaMalloc tail");
+  check(cudaMalloc(&t.rem, t.cap * sizeof(long long)), "cudaMalloc tail");
+  check(cudaMalloc(&t.lvl, (t.lvl_cap + 2) * sizeof(int)), "cudaMalloc tail");
+  check(cudaMalloc(&t.list, t.max_active * sizeof(long long)), "cudaMalloc tail");
+  check(cudaMalloc(&t.count, sizeof(unsigned)), "cudaMalloc tail");
+  check(cudaMemsetAsync(t.vis, 0, std::max<long long>(NP, 1) * sizeof(int), stream), "memset");
+  tail = t;
+  tail_stamp = 1;
 }
 
 PoolRunner::~PoolRunner() { release(); }
@@ -338,6 +376,13 @@ void PoolRunner::setup(const std::vector<InstDesc>& insts, cudaStream_t s) {
     threads = std::max(threads, I.g.TA * I.g.TB * I.g.TC);
     hv_max = std::max(hv_max, (I.g.TA + 2 * I.st.HA) * (I.g.TB + 2 * I.st.HB) * (I.g.TC + 2 * I.st.HC));
   }
+}
+
+// empty both tile lists so the next relabel starts clean
+void PoolRunner::drain_queue() {
+  check(cudaMemsetAsync(q.ctr, 0, 4 * sizeof(unsigned), stream), "memset");
+  for (int b = 0; b < 2; ++b)
+    check(cudaMemsetAsync(q.flag[b], 0, std::max(tiles, 1) * sizeof(int), stream), "memset");
 }
 
 void PoolRunner::prep_pass(int cur) {
@@ -432,13 +477,50 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   const size_t smem = pool_pr_smem<T>(KB, NTmax, hv_max);
   const long long max_epochs = 1000000;
   const auto t0 = std::chrono::steady_clock::now();
+  const bool trace = std::getenv("LF_PR_TRACE") != nullptr;  // diagnostic: one line per epoch
+  // tail steps per solve at most (each moves at least one unit; this bounds
+  // a run of steps that each move little), then the tile passes finish
+  const int kMaxTailSteps = 256;
+  int tail_steps = 0;
   for (long long epoch = 0;; ++epoch) {
     if (epoch > max_epochs) throw LfError{4, "push-relabel did not converge"};
     if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(300))
       throw LfError{4, "push-relabel exceeded its time limit"};
+    const long long bfs0 = stats.bfs_passes;
     global_relabel<T>(res, exc, h, mask, kmask, stats);
     ++stats.epochs;
-    if (activate<T>(exc, h) == 0) break;
+    const unsigned long long act = activate<T>(exc, h);
+    if (trace) {
+      unsigned long long c[2];
+      sync_read(c, d_counters, sizeof(c));
+      std::fprintf(stderr, "pr epoch %lld active %llu bfs %lld tiles %llu hmax0 %d\n", epoch, act,
+                   stats.bfs_passes - bfs0, c[0], n == 1 ? host[0].hmax : -1);
+    }
+    if (act == 0) break;
+    // few active nodes: route their excess along BFS trees to deficits
+    const int tail_max = tune.tail_active == 0 ? 64 : tune.tail_active;
+    if (tail_max > 0 && act <= (unsigned long long)tail_max && tail_steps < kMaxTailSteps) {
+      ++tail_steps;
+      alloc_tail();
+      if (tail_stamp > INT_MAX - 2 * tail.max_active) {  // restart the stamps
+        check(cudaMemsetAsync(tail.vis, 0, NP * sizeof(int), stream), "memset");
+        tail_stamp = 1;
+      }
+      mark(0, false);
+      check(launch_pool_tail<T>(d_inst, d_nbase, n, NP, res, exc, h, kmask, tail, tail_stamp,
+                                d_counters + 2, stream), "tail step");
+      mark(0, true);
+      count_launch();
+      count_launch();
+      tail_stamp += tail.max_active;
+      ++stats.tail_steps;
+      unsigned long long moved = 0;
+      sync_read(&moved, d_counters + 2, sizeof(moved));
+      if (moved > 0) {  // relabel again; else fall back to the tile passes
+        drain_queue();
+        continue;
+      }
+    }
     int cur = 0;
     for (int l = 0; l < M; ++l) {
       prep_pass(cur);
@@ -451,10 +533,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
       ++stats.pr_launches;
       cur ^= 1;
     }
-    // drain what the last pass queued so the next relabel starts clean
-    check(cudaMemsetAsync(q.ctr, 0, 4 * sizeof(unsigned), stream), "memset");
-    for (int b = 0; b < 2; ++b)
-      check(cudaMemsetAsync(q.flag[b], 0, std::max(tiles, 1) * sizeof(int), stream), "memset");
+    drain_queue();
   }
   if (sets) reach<T>(exc, mask, markv, stats);
   unsigned long long c[2];

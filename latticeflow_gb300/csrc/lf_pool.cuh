@@ -17,7 +17,9 @@ struct InstDesc {
   Geo g;
   Stencil st;
   long long node_base;  // first node of the lattice in the node pools
-  long long res_base;   // first element of its residual planes (K * NP)
+  long long res_base;   // first element of its residual planes
+  long long plane;      // elements between two residual planes (g.NP, or the
+                        // enclosing lattice's NP for a lattice stacked in it)
   int tile_base;        // global id of its tile 0
   int hmax;             // height cap of the current epoch
   int done;             // no node can push any more: excluded from relabels

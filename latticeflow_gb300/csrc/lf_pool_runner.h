@@ -21,10 +21,11 @@ struct Tuning {
   int launches_per_relabel = 0;  // push/relabel passes between global relabels
   int height_slack = 0;          // heights above (BFS depth + slack) park until the next relabel
   int pass_chunk = 0;            // BFS / closure passes launched between host checks
+  int tail_active = 0;           // active nodes at most for the tail step; 0 = 64, < 0 = off
 };
 
 struct SolveStats {
-  long long epochs = 0, pr_launches = 0, bfs_passes = 0, reach_passes = 0;
+  long long epochs = 0, pr_launches = 0, bfs_passes = 0, reach_passes = 0, tail_steps = 0;
   unsigned long long tiles_processed = 0, bfs_tiles = 0;
 };
 
@@ -37,6 +38,28 @@ struct ProfHooks {
 };
 
 size_t pool_smem_head_bytes();
+
+// Device scratch of the tail step (lf_pool_tail.cu): a BFS tree of at most
+// `cap` nodes and `lvl_cap` levels per active node, at most max_active
+// active nodes per step.
+struct TailScratch {
+  int* vis = nullptr;            // [NP] tree stamp per node
+  long long* node = nullptr;     // [cap] tree nodes in BFS order
+  int* par = nullptr;            // [cap] position of the parent
+  unsigned char* dir = nullptr;  // [cap] direction parent -> node
+  long long* dem = nullptr;      // [cap] demand / contribution
+  long long* rem = nullptr;      // [cap] flow still to pass on
+  int* lvl = nullptr;            // [lvl_cap + 2] first position of each level
+  long long* list = nullptr;     // [max_active] active nodes
+  unsigned* count = nullptr;     // active nodes found
+  int cap = 0, lvl_cap = 0, max_active = 0;
+};
+
+template <typename T>
+cudaError_t launch_pool_tail(const InstDesc* insts, const long long* nbase, int n, long long NP,
+                             T* res, T* exc, const int* h, const uint64_t* kmask,
+                             const TailScratch& s, int stamp0, unsigned long long* moved,
+                             cudaStream_t st);
 
 template <typename T>
 size_t pool_pr_smem(int K, int NT, int HV) {
@@ -100,6 +123,7 @@ class PoolRunner {
   template <typename T> unsigned long long activate(const T* exc, const int* h);
   template <typename T> void reach(const T* exc, const uint64_t* mask, int* mark, SolveStats& stats);
   void prep_pass(int cur);
+  void drain_queue();
   void sync_read(void* dst, const void* src, size_t bytes);
   void mark(int cat, bool end);
   void count_launch();
@@ -118,6 +142,10 @@ class PoolRunner {
   void* h_pin = nullptr;
   int threads = 1, hv_max = 0;
   int ka = 0, kb = 0;  // kernel sizes present in the pool
+  TailScratch tail;
+  int tail_stamp = 1;
+  void alloc_tail();
+  void free_tail();
   int grid_bfs = 0, grid_reach = 0;
 };
 

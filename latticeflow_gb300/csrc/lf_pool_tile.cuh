@@ -80,7 +80,7 @@ __device__ void pr_tile(const PoolPR<T>& p, const InstDesc& I, PoolSmemHead* hd,
   if (live) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      r0[k] = res[(long long)k * g.NP + x.gi];
+      r0[k] = res[(long long)k * I.plane + x.gi];
       s_res[k * NT + t] = r0[k];
       if (outside_tile(g, x, st.da[k], st.db[k], st.dc[k])) outm |= 1ull << k;
     }
@@ -146,16 +146,16 @@ __device__ void pr_tile(const PoolPR<T>& p, const InstDesc& I, PoolSmemHead* hd,
       if ((outm >> k) & 1) {
         const T d = r0[k] - rf;
         if (d != 0) {
-          atom_add(&res[(long long)k * g.NP + x.gi], (T)-d);
+          atom_add(&res[(long long)k * I.plane + x.gi], (T)-d);
           const int A_ = x.a0 + x.ia + st.da[k], B_ = x.b0 + x.ib + st.db[k],
                     C_ = x.c0 + x.ic + st.dc[k];
           const long long gn = ((long long)A_ * g.Bp + B_) * g.Cp + C_;
-          atom_add(&res[(long long)st.rev[k] * g.NP + gn], d);
+          atom_add(&res[(long long)st.rev[k] * I.plane + gn], d);
           atom_add(&exc[gn], d);
           enqueue_tile(p.q, nxt, I.tile_base + tile_of(g, A_, B_, C_));
         }
       } else {
-        res[(long long)k * g.NP + x.gi] = rf;
+        res[(long long)k * I.plane + x.gi] = rf;
       }
     }
     h[x.gi] = my_h;

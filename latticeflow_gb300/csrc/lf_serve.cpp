@@ -10,6 +10,11 @@
 //     same time on different streams and their kernels overlap on the device;
 //     a request arriving while others run is admitted as soon as a worker and
 //     memory free up;
+//   * TV requests of one kernel and shape waiting together are solved as one
+//     stacked problem (continuous batching): the worker that admits a TV
+//     request also takes up to max_group - 1 more of the same shape from the
+//     queue (a power-of-two group, so that few engine shapes are cached),
+//     within the HBM budget; each result equals the request's own solve;
 //   * latency = completion time - submission time (queueing included).
 // No reference counterpart (the reference solves one request per call).
 #include <algorithm>
@@ -72,10 +77,12 @@ struct Server::Impl {
 
   struct Worker {
     std::thread th;
-    std::map<std::tuple<bool, std::string, size_t, size_t>, std::unique_ptr<Engine>> engines;
+    std::map<std::tuple<bool, std::string, size_t, size_t, size_t>, std::unique_ptr<Engine>> engines;
   };
 
   size_t budget = 0, in_flight_bytes = 0;
+  int max_group = 8;
+  long long groups = 0, grouped = 0;
   int in_flight = 0, max_in_flight = 0;
   bool stop = false;
   int64_t next_id = 1;
@@ -95,48 +102,122 @@ struct Server::Impl {
     return in_flight_bytes + r.bytes <= budget;
   }
 
+  static bool same_shape(const Req& a, const Req& b) {
+    return a.tv && b.tv && a.kd == b.kd && a.nx == b.nx && a.ny == b.ny;
+  }
+
+  // With `mu` held: the front request plus, for a TV request, the queued TV
+  // requests of its shape that fit the budget (power-of-two group size).
+  std::vector<std::shared_ptr<Req>> take_group() {
+    std::vector<std::shared_ptr<Req>> g{queue.front()};
+    queue.pop_front();
+    size_t bytes = g[0]->bytes;
+    if (g[0]->tv && max_group > 1) {
+      std::vector<size_t> idx;
+      for (size_t i = 0; i < queue.size() && int(idx.size()) + 1 < max_group; ++i) {
+        if (!same_shape(*g[0], *queue[i])) continue;
+        if (in_flight_bytes + bytes + queue[i]->bytes > budget) break;
+        bytes += queue[i]->bytes;
+        idx.push_back(i);
+      }
+      size_t G = 1;
+      while (G * 2 <= idx.size() + 1) G *= 2;
+      idx.resize(G - 1);
+      for (size_t k = idx.size(); k-- > 0;) {
+        g.push_back(queue[idx[k]]);
+        queue.erase(queue.begin() + idx[k]);
+      }
+      std::reverse(g.begin() + 1, g.end());
+    }
+    return g;
+  }
+
   void work(Worker* w) {
     cudaSetDevice(device);
     for (;;) {
-      std::shared_ptr<Req> r;
+      std::vector<std::shared_ptr<Req>> grp;
+      size_t grp_bytes = 0;
       {
         std::unique_lock<std::mutex> lk(mu);
         cv_work.wait(lk, [&] { return stop || (!queue.empty() && admissible(*queue.front())); });
         if (stop && queue.empty()) return;
         if (queue.empty() || !admissible(*queue.front())) continue;
-        r = queue.front();
-        queue.pop_front();
-        in_flight_bytes += r->bytes;
-        ++in_flight;
+        grp = take_group();
+        const auto now = Clock::now();
+        for (auto& r : grp) {
+          grp_bytes += r->bytes;
+          r->t_start = now;
+        }
+        in_flight_bytes += grp_bytes;
+        in_flight += int(grp.size());
         max_in_flight = std::max(max_in_flight, in_flight);
-        r->t_start = Clock::now();
+        if (grp.size() > 1) {
+          ++groups;
+          grouped += (long long)grp.size();
+        }
       }
-      solve(w, *r);
+      if (grp.size() == 1) solve(w, *grp[0]);
+      else solve_group(w, grp);
       {
         std::lock_guard<std::mutex> lk(mu);
-        r->t_end = Clock::now();
-        r->done = true;
-        in_flight_bytes -= r->bytes;
-        --in_flight;
-        latencies.push_back(std::chrono::duration<double>(r->t_end - r->t_submit).count());
-        last_end = r->t_end;
+        const auto now = Clock::now();
+        for (auto& r : grp) {
+          r->t_end = now;
+          r->done = true;
+          latencies.push_back(std::chrono::duration<double>(r->t_end - r->t_submit).count());
+        }
+        in_flight_bytes -= grp_bytes;
+        in_flight -= int(grp.size());
+        last_end = now;
       }
       cv_done.notify_all();
       cv_work.notify_all();
     }
   }
 
+  // the worker's engine for `count` stacked TV problems (count 1 for a cut)
+  Engine& engine_for(Worker* w, bool tv, const KernelDef* kd, size_t nx, size_t ny,
+                     size_t count = 1) {
+    auto key = std::make_tuple(tv, kd->name, nx, ny, count);
+    auto it = w->engines.find(key);
+    if (it == w->engines.end()) {
+      size_t dims[2] = {nx, ny};
+      std::unique_ptr<Engine> e(tv ? new_tv_stack_engine(kd, nx, ny, count)
+                                   : new Engine("GPUPushRelabel", kd, 2, dims));
+      it = w->engines.emplace(key, std::move(e)).first;
+    }
+    return *it->second;
+  }
+
+  // TV requests of one shape as one stacked solve.
+  void solve_group(Worker* w, std::vector<std::shared_ptr<Req>>& grp) {
+    const Req& r0 = *grp[0];
+    const size_t G = grp.size(), N = r0.nx * r0.ny;
+    try {
+      Engine& E = engine_for(w, true, r0.kd, r0.nx, r0.ny, G);
+      std::vector<double> f(G * N), lam(G), out(G * N);
+      std::vector<int64_t> lv(G * N);
+      for (size_t p = 0; p < G; ++p) {
+        std::copy(grp[p]->f.begin(), grp[p]->f.end(), f.begin() + p * N);
+        lam[p] = grp[p]->lambda;
+      }
+      tv_2d_stack_on(E, r0.nx, r0.ny, G, f.data(), N, lam.data(), out.data(), lv.data());
+      for (size_t p = 0; p < G; ++p) {
+        Req& r = *grp[p];
+        r.out.assign(out.begin() + p * N, out.begin() + (p + 1) * N);
+        r.levels.assign(lv.begin() + p * N, lv.begin() + (p + 1) * N);
+        r.status = 0;
+      }
+    } catch (const LfError& e) {
+      for (auto& r : grp) { r->status = e.code; r->error = e.msg; }
+    } catch (const std::exception& e) {
+      for (auto& r : grp) { r->status = 7; r->error = e.what(); }
+    }
+  }
+
   void solve(Worker* w, Req& r) {
     try {
-      auto key = std::make_tuple(r.tv, r.kd->name, r.nx, r.ny);
-      auto it = w->engines.find(key);
-      if (it == w->engines.end()) {
-        size_t dims[2] = {r.nx, r.ny};
-        std::unique_ptr<Engine> e(
-            new Engine(r.tv ? "GPULevelReductions" : "GPUPushRelabel", r.kd, 2, dims));
-        it = w->engines.emplace(key, std::move(e)).first;
-      }
-      Engine& E = *it->second;
+      Engine& E = engine_for(w, r.tv, r.kd, r.nx, r.ny);
       if (r.tv) {
         r.out.resize(r.nx * r.ny);
         r.levels.resize(r.nx * r.ny);
@@ -274,6 +355,17 @@ void Server::release(int64_t id) {
   std::lock_guard<std::mutex> lk(impl->mu);
   auto it = impl->reqs.find(id);
   if (it != impl->reqs.end() && it->second->done) impl->reqs.erase(it);
+}
+
+void Server::set_max_group(int g) {
+  std::lock_guard<std::mutex> lk(impl->mu);
+  impl->max_group = std::max(1, g);
+}
+
+void Server::group_stats(long long* groups, long long* grouped) {
+  std::lock_guard<std::mutex> lk(impl->mu);
+  if (groups) *groups = impl->groups;
+  if (grouped) *grouped = impl->grouped;
 }
 
 void Server::stats(double* p50_ms, double* p99_ms, double* solves_per_s, long long* completed,

@@ -22,6 +22,9 @@ class Server {
   void get_tv(int64_t id, double* out, int64_t* levels);
   void get_cut(int64_t id, int* cut, long long* flow, long long* energy);
   void release(int64_t id);
+  // largest group of same-shape TV requests solved together (1 = none)
+  void set_max_group(int g);
+  void group_stats(long long* groups, long long* grouped);
   void stats(double* p50_ms, double* p99_ms, double* solves_per_s, long long* completed,
              long long* max_in_flight);
 

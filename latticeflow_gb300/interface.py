@@ -285,6 +285,55 @@ def calculate2dTV(f, lam, kernel="Full2d_4", return_levels=False):
     return (out, lv) if return_levels else out
 
 
+def calculate2dTVPath(f, lambdas, kernel="Full2d_4"):
+    """TV at every lambda (calculate2dTV with a lambda list,
+    tv/tv_solver.hpp:657-681) -> array [len(lambdas), nx, ny].
+
+    Slice i is the single-lambda solution at lambdas[i] (equal to
+    ``calculate2dTV(f, lambdas[i])``); all lambdas are solved together on the
+    GPU.  Negative lambdas count as 0, as in the reference.  (The Cython
+    wrappers also rescale their output, ``pylatticeflow.pyx:452`` by lambda
+    and ``:482`` by a stale lambda; these functions return the C++ entries'
+    values unscaled.)
+    """
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    if f.ndim != 2:
+        raise ValueError("calculate2dTVPath takes a 2-d array")
+    lam = np.ascontiguousarray(np.atleast_1d(lambdas), dtype=np.float64)
+    if lam.ndim != 1:
+        raise ValueError("lambdas must be a 1-d sequence")
+    nx, ny = f.shape
+    out = np.empty((lam.size, nx, ny), dtype=np.float64)
+    N.check(N.lib().lf_tv_2d_path(kernel.encode(), nx, ny, _p(f), lam.size, _p(lam), _p(out)))
+    return out
+
+
+def calculate2dTVBatch(images, lambdas, kernel="Full2d_4", return_levels=False, max_nodes=0):
+    """Many single-lambda TV problems of one shape solved together.
+
+    ``images``: array [count, nx, ny] (or one [nx, ny] image shared by all
+    problems); ``lambdas``: count values.  Result [count, nx, ny], slice p
+    equal to ``calculate2dTV(images[p], lambdas[p])``.
+    """
+    f = np.ascontiguousarray(images, dtype=np.float64)
+    lam = np.ascontiguousarray(np.atleast_1d(lambdas), dtype=np.float64)
+    if f.ndim == 2:
+        nx, ny = f.shape
+        stride = 0
+    elif f.ndim == 3:
+        if f.shape[0] != lam.size:
+            raise ValueError("one lambda per image")
+        nx, ny = f.shape[1:]
+        stride = nx * ny
+    else:
+        raise ValueError("images must be [nx, ny] or [count, nx, ny]")
+    out = np.empty((lam.size, nx, ny), dtype=np.float64)
+    lv = np.empty((lam.size, nx, ny), dtype=np.int64)
+    N.check(N.lib().lf_tv_2d_batch(kernel.encode(), nx, ny, lam.size, _p(f), stride, _p(lam),
+                                   _p(out), _p(lv), int(max_nodes)))
+    return (out, lv) if return_levels else out
+
+
 class LatticeBatch(object):
     """Many independent lattices solved together on the GPU (one instance pool).
 
@@ -383,13 +432,17 @@ class LatticeServer(object):
     until the request is finished and returns its latency in seconds;
     ``result`` returns the solution.  ``stats()`` gives p50 / p99 latency,
     throughput and the largest number of requests in flight together.
+    TV requests of one shape waiting together are solved as one stacked
+    problem (``max_group``, default 8; 1 turns grouping off).
     """
 
-    def __init__(self, workers=4, hbm_budget_bytes=0):
+    def __init__(self, workers=4, hbm_budget_bytes=0, max_group=None):
         h = ctypes.c_void_p()
         N.check(N.lib().lf_server_create(int(workers), int(hbm_budget_bytes), ctypes.byref(h)))
         self._h = h
         self._meta = {}
+        if max_group is not None:
+            N.check(N.lib().lf_server_set_max_group(h, int(max_group)))
 
     def close(self):
         h = getattr(self, "_h", None)
@@ -447,5 +500,8 @@ class LatticeServer(object):
         c, m = ctypes.c_int64(), ctypes.c_int64()
         N.check(N.lib().lf_server_stats(self._h, ctypes.byref(p50), ctypes.byref(p99),
                                         ctypes.byref(sps), ctypes.byref(c), ctypes.byref(m)))
+        g, gr = ctypes.c_int64(), ctypes.c_int64()
+        N.check(N.lib().lf_server_group_stats(self._h, ctypes.byref(g), ctypes.byref(gr)))
         return {"p50_ms": p50.value, "p99_ms": p99.value, "solves_per_s": sps.value,
-                "completed": c.value, "max_in_flight": m.value}
+                "completed": c.value, "max_in_flight": m.value, "groups": g.value,
+                "grouped_requests": gr.value}

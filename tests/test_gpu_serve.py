@@ -67,3 +67,25 @@ def test_server_budget_admission(native, gpu):
     with pytest.raises(lf.BadSolverOrKernelName):
         S.submit_tv(np.zeros((4, 4)), 1.0, kernel="Full2d_12")   # no geocut weights
     S.close()
+
+
+def test_server_groups_same_shape_tv(native, gpu, oracle_port):
+    """Same-shape TV requests queued behind a running one are solved as one
+    stacked problem; each result still equals its own solve."""
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    S = lf.LatticeServer(workers=1, max_group=4)
+    first = S.submit_tv(W.tv_image(90, n=256, polygons=8), 0.05)
+    reqs = [(W.tv_image(91 + i, n=64, polygons=4), lam)
+            for i, lam in enumerate([0.01, 0.2, 3.0, 0.05, 9.0, 0.7])]
+    ts = [S.submit_tv(f, lam) for f, lam in reqs]
+    S.wait(first)
+    for (f, lam), t in zip(reqs, ts):
+        S.wait(t)
+        out, lv = S.result(t)
+        ref, r, _ = oracle_port.port_tv_single("Full2d_4", f, lam)
+        assert int(np.abs(lv - r).max()) <= 1 and _tv_close(out, ref)
+    st = S.stats()
+    assert st["completed"] == 7
+    assert st["groups"] >= 1 and st["grouped_requests"] >= 2
+    S.close()
