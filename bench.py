@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--profile-run", action="store_true",
                     help="only warm-up and timed device-resident solves (for ncu captures)")
+    ap.add_argument("--tuning", default=None,
+                    help="tile_rows,local_sweeps,launches_per_relabel instead of the autotuner "
+                         "(e.g. the setting a bench run chose, for a profile run)")
     return ap.parse_args()
 
 
@@ -236,7 +239,12 @@ def run_ours(args):
         return ms, res, prof, launches
 
     tuning = None
-    if not args.no_autotune and not args.profile_run:
+    if args.tuning:
+        tr_, sw_, lp_ = (int(x) for x in args.tuning.split(","))
+        tuning = {"tile_rows": tr_, "local_sweeps": sw_, "launches_per_relabel": lp_}
+        for k_, v_ in tuning.items():
+            L.setParam(k_, v_)
+    elif not args.no_autotune and not args.profile_run:
         from latticeflow_gb300 import autotune
         step_device()
         tuning, _, _ = autotune.tune(L, autotune.problem_key([p.kernel], p.n))
@@ -284,7 +292,7 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generator, latticeflow_gb300/workloads.py)",
         "config": dict(workload_config(args.workload, p), parallelism="replicas" if world > 1 else "single",
-                       tuning=tuning, autotuned=tuning is not None),
+                       tuning=tuning, autotuned=tuning is not None and not args.tuning),
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT,
                 "h2d_bytes_per_step": int(u.nbytes + b.nbytes),
                 "d2h_bytes_per_step": int(2 * p.n * 4 + 64)},

@@ -247,7 +247,8 @@ int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double l
 /* calculate2dTV<Kernel, int64>(nx, ny, f, vector<double> lambdas)
  * (tv/tv_solver.hpp:657-681): the denoised image at every lambda,
  * out[n_lambda][nx][ny].  Slice i is the single-lambda solution at
- * lambdas[i] (what lf_tv_2d returns), all lambdas solved together.  The
+ * lambdas[i] (what lf_tv_2d returns), all lambdas solved together as
+ * lf_tv_2d_batch solves them.  The
  * reference traces the path instead with piecewise-linear region segments
  * (tv/tv_regpath_node.hpp), whose values differ from its own single-lambda
  * solutions away from the smallest lambdas.  As in the reference a negative
@@ -258,8 +259,10 @@ int lf_tv_2d_path(const char* kernel, size_t nx, size_t ny, const double* f, siz
 /* Many single-lambda TV problems of one shape solved together on the GPU:
  * problem p is the image at f + p * f_stride (f_stride = 0: one image for
  * all problems) at lambda lambdas[p]; out (and levels_out, may be NULL) hold
- * count * nx * ny values, problem-major.  max_nodes bounds the lattice nodes
- * of one stacked solve (0 = 2^26); larger batches run as several stacks.
+ * count * nx * ny values, problem-major.  Small problems are stacked into
+ * one lattice of at most max_nodes nodes (0 = 2^18; stacked problems advance
+ * in lockstep, so large ones are not stacked), and the stacks run as
+ * independent solves on up to 8 host threads with their own CUDA streams.
  * No reference counterpart (the reference solves one image per call). */
 int lf_tv_2d_batch(const char* kernel, size_t nx, size_t ny, size_t count, const double* f,
                    size_t f_stride, const double* lambdas, double* out, int64_t* levels_out,

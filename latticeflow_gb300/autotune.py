@@ -4,7 +4,8 @@ The knobs trade tile occupancy (tile rows), work per tile visit (local
 push/relabel sweeps) and global-relabel frequency (push/relabel passes
 between two global relabels).  Their best values depend on the kernel and the
 lattice sizes, so they are measured: every candidate is timed on the actual
-problem (device time of complete solves, best of ``repeats``), the fastest is
+problem (device time of complete solves: one untimed solve, then the median
+of ``repeats`` timed ones, so that a lucky single run does not win), the fastest is
 applied and remembered per key (kernel set and size class) in memory and,
 when ``cache_path`` is given, in a JSON file.  Results do not depend on the
 knobs (the cut sets are canonical), only the time does.
@@ -51,7 +52,7 @@ def _store(cache_path, table):
     os.replace(tmp, cache_path)
 
 
-def tune(solver, key, grid=None, repeats=2, cache_path=None, force=False):
+def tune(solver, key, grid=None, repeats=3, cache_path=None, force=False):
     """Choose and apply the fastest knob setting for ``solver``.
 
     ``solver`` is a ``LatticeFlow`` or ``LatticeBatch`` that is already
@@ -73,7 +74,9 @@ def tune(solver, key, grid=None, repeats=2, cache_path=None, force=False):
         setting = dict(zip(names, values))
         for k, v in setting.items():
             solver.setParam(k, v)
-        t = min(_timed(solver) for _ in range(repeats))
+        _timed(solver)  # first solve of a setting: kernel variants load, caches fill
+        ts = sorted(_timed(solver) for _ in range(max(1, repeats)))
+        t = ts[len(ts) // 2]
         timings.append((setting, t))
         if t < best_t:
             best, best_t = setting, t

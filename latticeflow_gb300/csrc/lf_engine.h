@@ -121,8 +121,9 @@ int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* le
 int tv_2d_stack_on(Engine& E, size_t nx, size_t ny, size_t count, const double* f,
                    size_t f_stride, const double* lambdas, double* out, int64_t* levels_out);
 size_t tv_stack_size(size_t nx, size_t ny, size_t count, size_t max_nodes);
+constexpr size_t kTVStackNodes = size_t(1) << 18;  // default bound of one TV stack
 int tv_2d_batch(const KernelDef* kd, size_t nx, size_t ny, size_t count, const double* f,
                 size_t f_stride, const double* lambdas, double* out, int64_t* levels_out,
-                size_t max_nodes);
+                size_t max_nodes, int workers = 0);
 
 }  // namespace lfg

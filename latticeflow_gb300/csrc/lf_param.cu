@@ -25,7 +25,10 @@
 #include <cstdlib>
 #include <climits>
 #include <cstring>
+#include <atomic>
 #include <memory>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "lf_engine.h"
@@ -532,27 +535,67 @@ size_t tv_stack_size(size_t nx, size_t ny, size_t count, size_t max_nodes) {
   return std::max<size_t>(per, 1);
 }
 
-// Many single-lambda TV problems of one shape, in stacks of at most
-// max_nodes lattice nodes (0: 2^26).
+// Many single-lambda TV problems of one shape.  Stacked problems advance in
+// lockstep generations (every generation waits for its slowest member), so
+// only small problems are stacked -- up to max_nodes lattice nodes per stack
+// (0: 2^18), where launch and synchronisation costs dominate -- and the
+// stacks run as independent solves on `workers` host threads (0: 8), each
+// with its own engine and CUDA stream, whose kernels overlap on the device.
 int tv_2d_batch(const KernelDef* kd, size_t nx, size_t ny, size_t count, const double* f,
                 size_t f_stride, const double* lambdas, double* out, int64_t* levels_out,
-                size_t max_nodes) {
+                size_t max_nodes, int workers) {
   const size_t N = nx * ny;
   if (N == 0 || count == 0) return 0;
-  if (max_nodes == 0) max_nodes = size_t(1) << 26;
+  if (max_nodes == 0) max_nodes = kTVStackNodes;
+  if (workers <= 0) workers = 8;
   const size_t per = tv_stack_size(nx, ny, count, max_nodes);
-  std::unique_ptr<Engine> E;
-  size_t E_count = 0;
-  for (size_t p0 = 0; p0 < count; p0 += per) {
-    const size_t m = std::min(per, count - p0);
-    if (!E || E_count != m) {
-      E.reset();
-      E.reset(new_tv_stack_engine(kd, nx, ny, m));
-      E_count = m;
+  const size_t stacks = (count + per - 1) / per;
+  const int W = int(std::min<size_t>(size_t(workers), stacks));
+  int device = 0;
+  cudaGetDevice(&device);
+  std::atomic<size_t> next{0};
+  std::mutex mu;
+  LfError first{0, ""};
+  bool failed = false;
+  auto work = [&]() {
+    cudaSetDevice(device);
+    std::unique_ptr<Engine> E;
+    size_t E_count = 0;
+    for (;;) {
+      const size_t s = next.fetch_add(1);
+      if (s >= stacks) return;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        if (failed) return;
+      }
+      const size_t p0 = s * per, m = std::min(per, count - p0);
+      try {
+        if (!E || E_count != m) {
+          E.reset();
+          E.reset(new_tv_stack_engine(kd, nx, ny, m));
+          E_count = m;
+        }
+        tv_2d_stack_on(*E, nx, ny, m, f + p0 * f_stride, f_stride, lambdas + p0, out + p0 * N,
+                       levels_out ? levels_out + p0 * N : nullptr);
+      } catch (const LfError& e) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!failed) { failed = true; first = e; }
+        return;
+      } catch (const std::exception& e) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!failed) { failed = true; first = LfError{7, e.what()}; }
+        return;
+      }
     }
-    tv_2d_stack_on(*E, nx, ny, m, f + p0 * f_stride, f_stride, lambdas + p0, out + p0 * N,
-                   levels_out ? levels_out + p0 * N : nullptr);
+  };
+  if (W <= 1) {
+    work();
+  } else {
+    std::vector<std::thread> th;
+    for (int w = 0; w < W; ++w) th.emplace_back(work);
+    for (auto& t : th) t.join();
   }
+  if (failed) throw first;
   return 0;
 }
 

@@ -4,6 +4,8 @@
 
 #include "lf_pool_runner.h"
 #include <algorithm>
+#include <mutex>
+#include <type_traits>
 
 #include "lf_pool_tile.cuh"
 
@@ -27,32 +29,44 @@ inline int occupancy_grid(Kern kernel, int threads, size_t smem) {
   return per * sms;
 }
 
+template <typename T, int A, int B, bool S>
+inline auto pr_kernel() {
+  if constexpr (std::is_same<T, int>::value) return k_pool_pr<A, B, S>;
+  else return k_pool_pr64<A, B, S>;
+}
+
 template <typename T>
 cudaError_t launch_pool_pr(const PoolPR<T>& p, int KA, int KB, int threads, size_t smem,
                            bool single, int grid, cudaStream_t s) {
+  // launches come from several host threads (server workers, TV batches)
+  static std::mutex mu;
 #define X(A, B)                                                                            \
   if (KA == A && KB == B) {                                                                \
+    auto kt = pr_kernel<T, A, B, true>();                                                  \
+    auto kf = pr_kernel<T, A, B, false>();                                                 \
     static bool attr = false;                                                              \
-    if (!attr) {                                                                           \
-      cudaFuncSetAttribute(k_pool_pr<T, A, B, true>,                                       \
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);       \
-      cudaFuncSetAttribute(k_pool_pr<T, A, B, false>,                                      \
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);       \
-      cudaFuncSetAttribute(k_pool_pr<T, A, B, true>,                                       \
-                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);           \
-      cudaFuncSetAttribute(k_pool_pr<T, A, B, false>,                                      \
-                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);           \
-      attr = true;                                                                         \
-    }                                                                                      \
     static int cap_t = 0, cap_f = 0;                                                       \
     static size_t cap_smem = 0;                                                            \
-    if (!cap_t || cap_smem != smem) {                                                      \
-      cap_t = occupancy_grid(k_pool_pr<T, A, B, true>, threads, smem);                     \
-      cap_f = occupancy_grid(k_pool_pr<T, A, B, false>, threads, smem);                    \
-      cap_smem = smem;                                                                     \
+    int ct, cf;                                                                            \
+    {                                                                                      \
+      std::lock_guard<std::mutex> lk(mu);                                                  \
+      if (!attr) {                                                                         \
+        cudaFuncSetAttribute(kt, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); \
+        cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); \
+        cudaFuncSetAttribute(kt, cudaFuncAttributePreferredSharedMemoryCarveout, 100);     \
+        cudaFuncSetAttribute(kf, cudaFuncAttributePreferredSharedMemoryCarveout, 100);     \
+        attr = true;                                                                       \
+      }                                                                                    \
+      if (!cap_t || cap_smem != smem) {                                                    \
+        cap_t = occupancy_grid(kt, threads, smem);                                         \
+        cap_f = occupancy_grid(kf, threads, smem);                                         \
+        cap_smem = smem;                                                                   \
+      }                                                                                    \
+      ct = cap_t;                                                                          \
+      cf = cap_f;                                                                          \
     }                                                                                      \
-    if (single) k_pool_pr<T, A, B, true><<<std::min(grid, cap_t), threads, smem, s>>>(p);  \
-    else k_pool_pr<T, A, B, false><<<std::min(grid, cap_f), threads, smem, s>>>(p);        \
+    if (single) kt<<<std::min(grid, ct), threads, smem, s>>>(p);                           \
+    else kf<<<std::min(grid, cf), threads, smem, s>>>(p);                                  \
     return cudaGetLastError();                                                             \
   }
   LF_POOL_PR_LIST(X)

@@ -10,11 +10,13 @@
 //     same time on different streams and their kernels overlap on the device;
 //     a request arriving while others run is admitted as soon as a worker and
 //     memory free up;
-//   * TV requests of one kernel and shape waiting together are solved as one
-//     stacked problem (continuous batching): the worker that admits a TV
-//     request also takes up to max_group - 1 more of the same shape from the
-//     queue (a power-of-two group, so that few engine shapes are cached),
-//     within the HBM budget; each result equals the request's own solve;
+//   * small TV requests of one kernel and shape waiting together are solved
+//     as one stacked problem (continuous batching): the worker that admits a
+//     TV request also takes up to max_group - 1 more of the same shape from
+//     the queue (a power-of-two group, so that few engine shapes are cached;
+//     the stack stays within kTVStackNodes nodes, since stacked problems
+//     advance in lockstep), within the HBM budget; each result equals the
+//     request's own solve;
 //   * latency = completion time - submission time (queueing included).
 // No reference counterpart (the reference solves one request per call).
 #include <algorithm>
@@ -112,9 +114,13 @@ struct Server::Impl {
     std::vector<std::shared_ptr<Req>> g{queue.front()};
     queue.pop_front();
     size_t bytes = g[0]->bytes;
-    if (g[0]->tv && max_group > 1) {
+    // stacked problems advance in lockstep generations: only small ones
+    const size_t n0 = g[0]->nx * g[0]->ny;
+    const int cap = int(std::min<size_t>(size_t(std::max(max_group, 1)),
+                                         std::max<size_t>(kTVStackNodes / std::max<size_t>(n0, 1), 1)));
+    if (g[0]->tv && cap > 1) {
       std::vector<size_t> idx;
-      for (size_t i = 0; i < queue.size() && int(idx.size()) + 1 < max_group; ++i) {
+      for (size_t i = 0; i < queue.size() && int(idx.size()) + 1 < cap; ++i) {
         if (!same_shape(*g[0], *queue[i])) continue;
         if (in_flight_bytes + bytes + queue[i]->bytes > budget) break;
         bytes += queue[i]->bytes;
