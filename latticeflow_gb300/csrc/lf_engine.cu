@@ -117,6 +117,7 @@ Engine::~Engine() {
   cudaFree(d_u64);
   cudaFree(d_sum);
   cudaFree(d_kmask);
+  cudaFree(d_cuts);
   if (h_pinned) cudaFreeHost(h_pinned);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
@@ -326,10 +327,13 @@ void Engine::run() {
     check(counted(launch_sum_pos<long long>(g.NP, (const long long*)d_exc, d_sum, stream)), "sum");
   }
   check(cudaEventRecord(ev1, stream), "event");
-  long long sums[2];
-  sync_read(sums, d_sum, sizeof(sums));
-  long long c0 = 0;
-  sync_read(&c0, d_c0, sizeof(c0));
+  // flow and energy: both reads, one synchronisation
+  long long* hp = reinterpret_cast<long long*>(h_pinned);
+  check(cudaMemcpyAsync(hp, d_sum, 2 * sizeof(long long), cudaMemcpyDeviceToHost, stream), "memcpy");
+  check(cudaMemcpyAsync(hp + 2, d_c0, sizeof(long long), cudaMemcpyDeviceToHost, stream), "memcpy");
+  check(cudaStreamSynchronize(stream), "sync");
+  const long long sums[2] = {hp[0], hp[1]};
+  const long long c0 = hp[2];
   float ms = 0;
   cudaEventElapsedTime(&ms, ev0, ev1);
   run_time = ms * 1e-3;
@@ -343,31 +347,30 @@ void Engine::run() {
   prof_cnt[3] = stats.reach_passes;
   prof_cnt[4] = launches;
   prof_cnt[5] = (long long)stats.bfs_tiles;
-  fetch_cuts();
+  extract_cuts();
   solved = true;
 }
 
-void Engine::fetch_cuts() {
-  cut_min_host.assign((size_t)N, 0);
-  cut_max_host.assign((size_t)N, 0);
+// Both cut sets, read off the final labels (closure marks and heights), stay
+// in HBM (d_cuts, row-major); get_cut copies the requested one straight to
+// the caller.
+void Engine::extract_cuts() {
   if (N == 0) return;
-  int* buf = nullptr;
-  check(cudaMallocAsync(&buf, 2 * (size_t)N * sizeof(int), stream), "cudaMallocAsync");
-  check(counted(launch_extract_cuts(g, nd, N, d_mark, d_h, buf, buf + N, stream)), "extract cuts");
-  check(cudaMemcpyAsync(cut_min_host.data(), buf, N * sizeof(int), cudaMemcpyDeviceToHost, stream), "memcpy");
-  check(cudaMemcpyAsync(cut_max_host.data(), buf + N, N * sizeof(int), cudaMemcpyDeviceToHost, stream), "memcpy");
-  cudaFreeAsync(buf, stream);
-  check(cudaStreamSynchronize(stream), "sync");
+  if (!d_cuts) check(cudaMalloc(&d_cuts, 2 * (size_t)N * sizeof(int)), "cudaMalloc cuts");
+  check(counted(launch_extract_cuts(g, nd, N, d_mark, d_h, d_cuts, d_cuts + N, stream)),
+        "extract cuts");
 }
 
-void Engine::get_cut(int* out, bool maximal) const {
+void Engine::get_cut(int* out, bool maximal) {
   if (!solved) throw LfError{8, "getCut called before run"};
   if (parametric) {
     for (long long i = 0; i < N; ++i) out[i] = levels_host[i] < 0 ? 1 : 0;
     return;
   }
-  const std::vector<int>& v = maximal ? cut_max_host : cut_min_host;
-  std::memcpy(out, v.data(), N * sizeof(int));
+  if (N == 0) return;
+  check(cudaMemcpyAsync(out, d_cuts + (maximal ? N : 0), N * sizeof(int), cudaMemcpyDeviceToHost,
+                        stream), "memcpy");
+  check(cudaStreamSynchronize(stream), "sync");
 }
 
 void Engine::get_levels(int64_t* out) const {

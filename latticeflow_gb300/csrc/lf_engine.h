@@ -61,7 +61,7 @@ class Engine : public ProfHooks {
   void clear();
   void add_caps(const int32_t* src, const int32_t* snk, const int32_t* edge);
   void run();
-  void get_cut(int* out, bool maximal) const;
+  void get_cut(int* out, bool maximal);
   void get_levels(int64_t* out) const;
 
   bool solved = false;
@@ -96,7 +96,7 @@ class Engine : public ProfHooks {
   void mark(int cat, bool end) override;
   void prof_collect();
   cudaError_t counted(cudaError_t e) { ++launches; return e; }
-  std::vector<int> cut_min_host, cut_max_host;
+  int* d_cuts = nullptr;  // [2N] minimal / maximal on-set, filled by extract_cuts
   std::vector<int64_t> levels_host;
 
   void choose_geometry(int elem);
@@ -106,7 +106,7 @@ class Engine : public ProfHooks {
   void sync_read(void* host, const void* dev, size_t bytes);
   void check(cudaError_t e, const char* what) const;
   void free_working();
-  void fetch_cuts();
+  void extract_cuts();
 };
 
 void engine_run_parametric(Engine& E);  // lf_param.cu
