@@ -151,7 +151,8 @@ def measured_peaks():
 
 
 def committed_traffic(kernel_key):
-    """DRAM bytes per launch from the committed ncu summary, if present."""
+    """DRAM bytes per node visit of a kernel from a committed ncu capture
+    (profiles/traffic.json, keyed workload:kernel:tile), if present."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(path):
         with open(path) as f:
@@ -251,14 +252,22 @@ def run_ours(args):
         from latticeflow_gb300 import autotune
         step_device()
         tuning, _, tune_table = autotune.tune(L, autotune.problem_key([p.kernel], p.n))
+    if args.profile_run:
+        # every solve of the run (warm-up included), with the tile counters
+        # that turn a capture's DRAM bytes into bytes per node visit
+        tot = {"pr_tiles": 0, "pr_launches": 0, "bfs_tiles": 0, "bfs_passes": 0}
+        for _ in range(args.warmup + args.steps):
+            step_device()
+            pr = L.profile()
+            for k in tot:
+                tot[k] += pr[k]
+        torch.cuda.synchronize()
+        tile, _, elem = L.layout()
+        print(json.dumps(dict(profile_run=True, flow=L.flow()[0], solves=args.warmup + args.steps,
+                              tile=list(tile), elem_bytes=elem, tuning=tuning, **tot)))
+        return
     for _ in range(args.warmup):
         step_device()
-    if args.profile_run:
-        for _ in range(args.steps):
-            step_device()
-        torch.cuda.synchronize()
-        print(json.dumps({"profile_run": True, "flow": L.flow()[0]}))
-        return
     sampler = ClockSampler(local)
     sampler.start()
     # value: plain timed steps; then the same steps with CUDA events around
@@ -284,11 +293,15 @@ def run_ours(args):
     else:
         kname, kbytes, kms, klaunch = "k_pool_bfs", bfs_bytes, prof["bfs_ms"], prof["bfs_passes"]
     achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else 0.0
-    tr = committed_traffic(args.workload + ":" + kname)
+    tr = committed_traffic("%s:%s:%s" % (args.workload, kname, "x".join(str(v) for v in tile)))
+    klaunch_nodes = (prof["pr_tiles"] if kname == "k_pool_pr" else prof["bfs_tiles"]) * nt / max(1, klaunch)
     roofline = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs, copy)",
-                "traffic": tr.get("dram_bytes_per_launch") if tr else None,
+                # DRAM bytes per node visit from a committed ncu capture of the
+                # same kernel and workload, times this run's node visits per launch
+                "traffic": int(tr["dram_bytes_per_node_visit"] * klaunch_nodes) if tr else None,
+                "traffic_source": tr.get("source") if tr else "no committed capture for this tile shape",
                 "algorithmic_bytes_per_launch": int(kbytes / max(1, klaunch)),
                 "kernel_ms_share": round(kms / max(ms_prof, 1e-9), 3),
                 "launches": int(klaunch)}
