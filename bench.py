@@ -163,6 +163,25 @@ def committed_traffic(kernel_key):
     return None
 
 
+def max_over_ranks(x):
+    """The largest x over all ranks (replicas time their own work; the job
+    takes as long as the slowest).  One process: x itself."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank, world, seconds):
+    """Whole-job throughput of `world` replicas: all units over the
+    max-over-ranks time."""
+    return world * units_per_rank / seconds
+
+
 # ---------------------------------------------------------------- ours
 
 def run_ours(args):
@@ -233,11 +252,7 @@ def run_ours(args):
         ms = e0.elapsed_time(e1)
         launches = L.profile()["kernel_launches"] - k0
         L.setProfiling(False)
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms)
         barrier()
         return ms, res, prof, launches
 
@@ -306,8 +321,8 @@ def run_ours(args):
                 "kernel_ms_share": round(kms / max(ms_prof, 1e-9), 3),
                 "launches": int(klaunch)}
 
-    value = world * args.steps / (ms * 1e-3)
-    e2e_value = world * args.steps / (ms_e2e * 1e-3)
+    value = replica_value(args.steps, world, ms * 1e-3)
+    e2e_value = replica_value(args.steps, world, ms_e2e * 1e-3)
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
@@ -395,6 +410,9 @@ def run_batch(args):
     import torch
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     from latticeflow_gb300 import _build
     _build.build_native()
     import latticeflow_gb300 as lf
@@ -433,10 +451,12 @@ def run_batch(args):
             cut_bytes += B.getCut(i).nbytes
     wall_e2e = time.perf_counter() - t0
     n = len(probs)
+    dev, wall, wall_e2e = max_over_ranks(dev), max_over_ranks(wall), max_over_ranks(wall_e2e)
     summary = batch_summary(args) if rank == 0 else None
     h2d = int(sum(p.source.nbytes + p.sink.nbytes + p.edge.nbytes for p in probs))
     out = {
-        "metric": METRIC, "value": round(n * args.steps / dev, 3), "unit": UNIT, "n_gpus": world,
+        "metric": METRIC, "value": round(replica_value(n * args.steps, world, dev), 3), "unit": UNIT,
+        "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dev / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generator, latticeflow_gb300/workloads.py)",
@@ -444,7 +464,7 @@ def run_batch(args):
                    "sides": "log-uniform [64, 1024] per axis", "capacity": "int32",
                    "tuning": setting, "autotuned": setting is not None,
                    "l2": "inputs larger than L2 (no flush needed)"},
-        "e2e": {"value": round(n * args.steps / wall_e2e, 3), "unit": UNIT,
+        "e2e": {"value": round(replica_value(n * args.steps, world, wall_e2e), 3), "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(cut_bytes / args.steps)},
         "wall_ms_per_step": round(1e3 * wall / args.steps, 3),
         "clocks": clocks,
@@ -463,6 +483,9 @@ def run_serve(args):
     import torch
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     from latticeflow_gb300 import _build
     _build.build_native()
     import latticeflow_gb300 as lf
@@ -497,7 +520,7 @@ def run_serve(args):
     for t in tickets:
         lat.append(S.wait(t))
         S.release(t)
-    makespan = time.perf_counter() - t0
+    makespan = max_over_ranks(time.perf_counter() - t0)
     clocks = sampler.stop()
     st = S.stats()
     S.close()
@@ -510,7 +533,8 @@ def run_serve(args):
             per_size[str(n)] = {"count": int(m.sum()), "p50_ms": round(float(np.percentile(l, 50)), 2),
                                 "p99_ms": round(float(np.percentile(l, 99)), 2)}
     out = {
-        "metric": METRIC, "value": round(args.requests / makespan, 3), "unit": "solves/s",
+        "metric": METRIC, "value": round(replica_value(args.requests, world, makespan), 3),
+        "unit": "solves/s",
         "n_gpus": world, "steps": args.requests, "warmup": len(warm),
         "ms_per_step": round(1e3 * makespan / args.requests, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int64",
@@ -588,11 +612,8 @@ def run_tv_path(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
-    if world > 1:
-        t = torch.tensor([wall], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        wall = float(t.item())
-    value = world * args.steps * len(lams) / wall
+    wall = max_over_ranks(wall)
+    value = replica_value(args.steps * len(lams), world, wall)
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "lambda solves/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

@@ -303,6 +303,7 @@ void Engine::run() {
     return;
   }
   alloc_accumulators();
+  solved = false;  // a solve that fails leaves no result behind
   stats = SolveStats();
   for (int i = 0; i < 4; ++i) prof_ms[i] = 0;
   for (int i = 0; i < 6; ++i) prof_cnt[i] = 0;

@@ -475,7 +475,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   const int KA = ka, KB = kb;
   const int NTmax = threads;
   const size_t smem = pool_pr_smem<T>(KB, NTmax, hv_max);
-  const long long max_epochs = 1000000;
+  const long long max_epochs = tune.max_epochs > 0 ? tune.max_epochs : 1000000;
   const auto t0 = std::chrono::steady_clock::now();
   const bool trace = std::getenv("LF_PR_TRACE") != nullptr;  // diagnostic: one line per epoch
   // tail steps per solve at most (each moves at least one unit; this bounds
@@ -483,7 +483,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   const int kMaxTailSteps = 256;
   int tail_steps = 0;
   for (long long epoch = 0;; ++epoch) {
-    if (epoch > max_epochs) throw LfError{4, "push-relabel did not converge"};
+    if (epoch >= max_epochs) throw LfError{4, "push-relabel did not converge"};
     if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(300))
       throw LfError{4, "push-relabel exceeded its time limit"};
     const long long bfs0 = stats.bfs_passes;

@@ -22,6 +22,7 @@ struct Tuning {
   int height_slack = 0;          // heights above (BFS depth + slack) park until the next relabel
   int pass_chunk = 0;            // BFS / closure passes launched between host checks
   int tail_active = 0;           // active nodes at most for the tail step; 0 = 64, < 0 = off
+  int max_epochs = 0;            // global relabels per solve at most; 0 = 1,000,000
 };
 
 struct SolveStats {
