@@ -241,6 +241,7 @@ int lf_set_param(lf_lattice* h, const char* name, int value) {
     else if (n == "pass_chunk") t.pass_chunk = value;
     else if (n == "tail_active") t.tail_active = value;
     else if (n == "max_epochs") t.max_epochs = value;
+    else if (n == "tail_tree_nodes") t.tail_tree_nodes = value;
     else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
   });
 }
@@ -550,6 +551,7 @@ int lf_batch_set_param(lf_batch* b, const char* name, int value) {
     else if (n == "pass_chunk") t.pass_chunk = value;
     else if (n == "tail_active") t.tail_active = value;
     else if (n == "max_epochs") t.max_epochs = value;
+    else if (n == "tail_tree_nodes") t.tail_tree_nodes = value;
     else if (n == "defer_checks") b->b->defer_checks = value != 0;
     else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
   });

@@ -300,9 +300,12 @@ void PoolRunner::free_tail() {
 
 // Tail scratch, allocated at the first tail step of this pool.
 void PoolRunner::alloc_tail() {
-  if (tail.vis) return;
+  const long long want = std::min<long long>(
+      std::max<long long>(NP, 1), tune.tail_tree_nodes > 0 ? tune.tail_tree_nodes : 65536);
+  if (tail.vis && tail.cap == want) return;
+  if (tail.vis) free_tail();
   TailScratch t;
-  t.cap = int(std::min<long long>(std::max<long long>(NP, 1), 1LL << 22));
+  t.cap = int(want);
   t.lvl_cap = 1 << 16;
   t.max_active = 64;
   check(cudaMalloc(&t.vis, std::max<long long>(NP, 1) * sizeof(int)), "cudaMalloc tail");

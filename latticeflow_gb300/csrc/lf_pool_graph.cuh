@@ -15,6 +15,45 @@
 
 namespace lfg {
 
+// Distances along one tile row (the 32 lanes of a warp hold its 32 nodes):
+// a node that can push to its left neighbour (can = residual in that
+// direction) is at most that neighbour's distance + 1.  Segmented min-scan
+// of (h - lane) from the left; a lane that cannot push left starts a
+// segment.  Lane 0's left neighbour lies in the halo and is relaxed by the
+// ordinary stencil step.  Values at or above kHInf stay there (min with h).
+__device__ __forceinline__ int row_scan_from_left(int h, bool can, int lane) {
+  int v = h - lane;
+  bool head = !can || lane == 0;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int vu = __shfl_up_sync(0xffffffffu, v, off);
+    const int hu = __shfl_up_sync(0xffffffffu, (int)head, off);
+    if (lane >= off && !head) {
+      v = vu < v ? vu : v;
+      head = hu;
+    }
+  }
+  const int r = v + lane;
+  return r < h ? r : h;
+}
+
+// The same from the right (pushes to the right neighbour).
+__device__ __forceinline__ int row_scan_from_right(int h, bool can, int lane) {
+  int v = h + lane;
+  bool head = !can || lane == 31;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int vd = __shfl_down_sync(0xffffffffu, v, off);
+    const int hd = __shfl_down_sync(0xffffffffu, (int)head, off);
+    if (lane + off < 32 && !head) {
+      v = vd < v ? vd : v;
+      head = hd;
+    }
+  }
+  const int r = v - lane;
+  return r < h ? r : h;
+}
+
 template <int K>
 __device__ __forceinline__ void bfs_tile(const PoolBFS& p, const InstDesc& I, PoolSmemHead* hd,
                                          int* s_h, int gtile) {
@@ -30,12 +69,20 @@ __device__ __forceinline__ void bfs_tile(const PoolBFS& p, const InstDesc& I, Po
   int hoff[K];
   uint64_t m = 0;
   bool boundary = false;
+  int kl = -1, kr = -1;  // the directions along the row, if the stencil has them
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     hoff[k] = (st.da[k] * x.HBB + st.db[k]) * x.HCC + st.dc[k];
     if (outside_tile(g, x, st.da[k], st.db[k], st.dc[k])) boundary = true;
+    if (st.da[k] == 0 && st.db[k] == 0) {
+      if (st.dc[k] == -1) kl = k;
+      if (st.dc[k] == 1) kr = k;
+    }
   }
   if (live) m = p.mask[I.node_base + x.gi];
+  const bool can_l = kl >= 0 && ((m >> kl) & 1);
+  const bool can_r = kr >= 0 && ((m >> kr) & 1);
+  const int lane = x.ic;  // tiles are 32 nodes wide: one warp per row
   __syncthreads();
   int my_h = live ? s_h[x.hidx] : kHInf;
   bool changed = false;
@@ -49,6 +96,9 @@ __device__ __forceinline__ void bfs_tile(const PoolBFS& p, const InstDesc& I, Po
         best = hn < best ? hn : best;
       }
     }
+    // whole rows at once: every lane of the warp takes part
+    if (kl >= 0) best = row_scan_from_left(best, can_l, lane);
+    if (kr >= 0) best = row_scan_from_right(best, can_r, lane);
     const int c = best < my_h;
     if (c) {
       my_h = best;

@@ -23,6 +23,7 @@ struct Tuning {
   int pass_chunk = 0;            // BFS / closure passes launched between host checks
   int tail_active = 0;           // active nodes at most for the tail step; 0 = 64, < 0 = off
   int max_epochs = 0;            // global relabels per solve at most; 0 = 1,000,000
+  int tail_tree_nodes = 0;       // nodes of one tail-step tree at most; 0 = 65,536
 };
 
 struct SolveStats {
