@@ -151,7 +151,8 @@ int lf_set_tuning(lf_lattice* h, int tile_rows, int local_sweeps, int launches_p
 /* One knob by name: "tile_rows", "local_sweeps", "launches_per_relabel",
  * "height_slack", "pass_chunk", "tail_active" (at most this many active
  * nodes switch an epoch to routing their excess along BFS trees; 0 = 64,
- * negative = never), "max_epochs" (global relabels per solve before the
+ * negative = never), "tail_tree_nodes" (nodes of one such tree at most;
+ * 0 = 65,536), "max_epochs" (global relabels per solve before the
  * solve gives up with LF_ERR_NO_CONVERGENCE; 0 = 1,000,000; the handle stays
  * usable).  LF_ERR_INVALID for an unknown name. */
 int lf_set_param(lf_lattice* h, const char* name, int value);

@@ -91,7 +91,9 @@ __device__ void pr_tile(const PoolPR<T>& p, const InstDesc& I, PoolSmemHead* hd,
   int my_h = live ? s_h[x.hidx] : kHInf;
   for (int it = 0; it < p.sweeps; ++it) {
     T e = live ? s_exc[t] : (T)0;
-    if (e > 0 && my_h < hmax) {
+    // a node parked at the epoch cap no longer relabels but still pushes
+    // downhill (a lower neighbour may be a deficit)
+    if (e > 0) {
       T sent = 0;
 #pragma unroll
       for (int k = 0; k < K; ++k) {
