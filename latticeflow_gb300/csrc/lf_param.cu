@@ -246,12 +246,15 @@ void engine_run_parametric(Engine& E) {
   // problems: 6.7x fewer milliseconds at 1024^2 than the binary-cut setting).
   if (E.tune.sweeps <= 0) E.tune.sweeps = 16;
   if (E.tune.launches_per_relabel <= 0) E.tune.launches_per_relabel = 64;
-  // The tail step (BFS trees from the last active nodes) pays for binary
-  // cuts; section solves leave small deficits spread over large sections,
-  // so its trees span whole sections and cost more than the passes they save
-  // (measured at 1024^2, lambda = 0.05: 1.45 s -> 3.3 s with unbounded trees,
-  // 4.6 s with trees of at most 65,536 nodes).
-  if (E.tune.tail_active == 0) E.tune.tail_active = -1;
+  // Tail step only when a single node is still active, with trees as large
+  // as a section: after a generation's flow the remainder can sit in one
+  // node beside a million nodes short of one unit each, which the tile
+  // passes fill a few hundred per relabel.  With more roots the trees of a
+  // section solve cost more than the passes they save.  Measured at 1024^2:
+  // lambda = 1e-3 2.7 s -> 0.55 s, 0.05 1.58 -> 1.34 s, 1: 0.9 s either way;
+  // 64 lambdas 25.9 -> 20.8 s (4 roots: 22.9 s, 64 roots: 169 s).
+  if (E.tune.tail_active == 0) E.tune.tail_active = 1;
+  if (E.tune.tail_tree_nodes == 0) E.tune.tail_tree_nodes = 1 << 22;
   E.alloc_accumulators();
   E.stats = SolveStats();
   E.prepare_working(8);
