@@ -31,8 +31,8 @@ inline int occupancy_grid(Kern kernel, int threads, size_t smem) {
 
 template <typename T, int A, int B, bool S>
 inline auto pr_kernel() {
-  if constexpr (std::is_same<T, int>::value) return k_pool_pr<A, B, S>;
-  else return k_pool_pr64<A, B, S>;
+  if constexpr (std::is_same<T, int>::value && B <= 8) return k_pool_pr<A, B, S>;
+  else return k_pool_pr_wide<T, A, B, S>;
 }
 
 template <typename T>

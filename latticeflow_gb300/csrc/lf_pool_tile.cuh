@@ -185,17 +185,19 @@ __device__ __forceinline__ void pool_pr_body(const PoolPR<T>& p) {
   }
 }
 
-// 32-bit capacities: at most 40 registers, so three 512-thread tiles share an
-// SM (measured: push/relabel passes 11% faster than at 60 registers).
+// 32-bit capacities, at most 8 directions: at most 40 registers, so three
+// 512-thread tiles share an SM (measured: push/relabel passes 11% faster
+// than at 60 registers).
 template <int KA, int KB, bool SINGLE>
 __global__ void __maxnreg__(40) k_pool_pr(PoolPR<int> p) {
   pool_pr_body<int, KA, KB, SINGLE>(p);
 }
 
-// 64-bit capacities: no register cap (the cap spills to local memory).
-template <int KA, int KB, bool SINGLE>
-__global__ void __launch_bounds__(1024) k_pool_pr64(PoolPR<long long> p) {
-  pool_pr_body<long long, KA, KB, SINGLE>(p);
+// 64-bit capacities or larger kernels: no register cap (the cap spills to
+// local memory there).
+template <typename T, int KA, int KB, bool SINGLE>
+__global__ void __launch_bounds__(1024) k_pool_pr_wide(PoolPR<T> p) {
+  pool_pr_body<T, KA, KB, SINGLE>(p);
 }
 
 }  // namespace lfg
