@@ -180,11 +180,33 @@ void Engine::sync_read(void* host, const void* dev, size_t bytes) {
   std::memcpy(host, h_pinned, bytes);
 }
 
+// Device address of host memory the GPU reads in place (pinned, mapped into
+// the device's address space; on GB300 the reads go over NVLink-C2C), else
+// null (pageable memory is copied first).
+static const void* mapped_host_ptr(const void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the error of an unknown pointer
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device_ptrs) {
   alloc_accumulators();
   const int64_t *du = unary, *db = binary;
   int64_t *tu = nullptr, *tb = nullptr;
   size_t ub = (size_t)N * 2 * sizeof(int64_t), bb = (size_t)N * (st.K / 2) * 4 * sizeof(int64_t);
+  // pinned caller arrays: the fill kernel reads them in place, so the
+  // transfer overlaps the fill instead of preceding it
+  const int64_t* mu = device_ptrs ? nullptr : (const int64_t*)mapped_host_ptr(unary);
+  const int64_t* mb = device_ptrs ? nullptr : (const int64_t*)mapped_host_ptr(binary);
+  if (mu && mb) {
+    du = mu;
+    db = mb;
+    device_ptrs = true;
+  }
   if (!device_ptrs) {
     check(cudaMallocAsync(&tu, ub, stream), "cudaMallocAsync unary");
     check(cudaMallocAsync(&tb, bb, stream), "cudaMallocAsync binary");
@@ -213,9 +235,16 @@ void Engine::add_caps(const int32_t* src, const int32_t* snk, const int32_t* edg
   size_t nb = (size_t)N * sizeof(int32_t), eb = (size_t)N * (st.K / 2) * sizeof(int32_t);
   check(cudaMallocAsync(&buf, 2 * nb + eb, stream), "cudaMallocAsync caps");
   int32_t *ds = nullptr, *dt = nullptr, *de = nullptr;
-  if (src) { ds = buf; check(cudaMemcpyAsync(ds, src, nb, cudaMemcpyHostToDevice, stream), "memcpy"); }
-  if (snk) { dt = buf + N; check(cudaMemcpyAsync(dt, snk, nb, cudaMemcpyHostToDevice, stream), "memcpy"); }
-  if (edge) { de = buf + 2 * N; check(cudaMemcpyAsync(de, edge, eb, cudaMemcpyHostToDevice, stream), "memcpy"); }
+  // pinned caller arrays are read in place (see add_energy)
+  auto in = [&](const int32_t* h, int32_t* stage, size_t bytes) -> int32_t* {
+    if (!h) return nullptr;
+    if (const void* m = mapped_host_ptr(h)) return (int32_t*)m;
+    check(cudaMemcpyAsync(stage, h, bytes, cudaMemcpyHostToDevice, stream), "memcpy");
+    return stage;
+  };
+  ds = in(src, buf, nb);
+  dt = in(snk, buf + N, nb);
+  de = in(edge, buf + 2 * N, eb);
   check(counted(launch_fill_caps(g, st, nd, N, ds, dt, de, d_exc64, d_cap64, d_c0, d_err,
                                  parametric ? 1 : 0, stream)),
         "fill caps");

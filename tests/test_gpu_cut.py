@@ -186,3 +186,39 @@ def test_tuning_does_not_change_result(native, gpu, oracle_port, tuning):
     L = solve(p.kernel, p.dims, u, b, tuning=tuning)
     assert L.flow()[1] == E
     assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
+
+
+def test_pinned_host_arrays_read_in_place(native, gpu):
+    """Pinned host energies / capacities are read by the fill kernels in
+    place; the result equals the copied (pageable) path bit for bit."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import _native as N
+    from latticeflow_gb300 import workloads as W
+    p = W.plain_cut(21, (150, 170), "Full2d_8")
+    u, b = p.energies()
+    pu = torch.from_numpy(u).pin_memory()
+    pb = torch.from_numpy(b).pin_memory()
+    a = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    N.check(N.lib().lf_add_energy_potentials(a._h, ctypes.c_void_p(pu.data_ptr()),
+                                             ctypes.c_void_p(pb.data_ptr())))
+    a.run()
+    c = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    N.check(N.lib().lf_add_energy_potentials(c._h, u.ctypes.data_as(ctypes.c_void_p),
+                                             b.ctypes.data_as(ctypes.c_void_p)))
+    c.run()
+    assert a.flow() == c.flow()
+    assert np.array_equal(a.getCut(), c.getCut()) and np.array_equal(a.getCutMax(), c.getCutMax())
+    # capacities
+    ps = torch.from_numpy(p.source).pin_memory()
+    pk = torch.from_numpy(p.sink).pin_memory()
+    pe = torch.from_numpy(np.ascontiguousarray(p.edge)).pin_memory()
+    d = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    N.check(N.lib().lf_add_capacities(d._h, ctypes.c_void_p(ps.data_ptr()), ctypes.c_void_p(pk.data_ptr()),
+                                      ctypes.c_void_p(pe.data_ptr())))
+    d.run()
+    e = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    e.addCapacities(p.source, p.sink, p.edge)
+    e.run()
+    assert d.flow() == e.flow() and np.array_equal(d.getCut(), e.getCut())
