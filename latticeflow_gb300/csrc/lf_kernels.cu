@@ -1,6 +1,7 @@
 // Per-lattice element kernels: energy / capacity fill, range bound, type
 // conversion, reductions and cut extraction.  The solve itself runs on the
 // pool kernels (lf_pool_tile.cuh, lf_pool.cu).
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -154,11 +155,23 @@ __global__ void k_convert(long long n, const long long* src, T* dst) {
 // sum of max(x, 0) over n values (int64 result)
 template <typename T>
 __global__ void k_sum_pos(long long n, const T* x, long long* out) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  // grid-stride partial sums, one atomic per block (not per warp: a
+  // lattice-wide sum otherwise queues ~N/32 atomics on one address)
+  __shared__ long long part[32];
   long long v = 0;
-  if (i < n) { T a = x[i]; v = a > 0 ? (long long)a : 0; }
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const T a = x[i];
+    if (a > 0) v += (long long)a;
+  }
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0 && v) atom_add(out, v);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0 && v) atom_add(out, v);
+  }
 }
 
 // Bounded (row-major) outputs: cut_min from marks, cut_max from h == kHInf.
@@ -220,7 +233,7 @@ template cudaError_t launch_convert<long long>(long long, const long long*, long
 
 template <typename T>
 cudaError_t launch_sum_pos(long long n, const T* x, long long* out, cudaStream_t s) {
-  if (n > 0) k_sum_pos<T><<<nblk(n, 256), 256, 0, s>>>(n, x, out);
+  if (n > 0) k_sum_pos<T><<<std::min(nblk(n, 256), 152 * 8), 256, 0, s>>>(n, x, out);
   return cudaGetLastError();
 }
 template cudaError_t launch_sum_pos<int>(long long, const int*, long long*, cudaStream_t);

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "lf_pool_runner.h"
 #include "lf_pool_tile.cuh"
@@ -123,6 +124,51 @@ __global__ void k_pool_active(const InstDesc* insts, const long long* nbase, int
   if (inst >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) {
     if (hm) atomicMax(&hmx[inst], hm);
     if (na) atomicAdd(&cnt[inst], (unsigned long long)na);
+  }
+}
+
+// The same for a pool of one lattice: no lattice lookup per node, the
+// active tiles queued once per warp (a warp's 32 nodes are one tile row),
+// count and maximum height combined per block.
+template <typename T>
+__global__ void k_pool_active1(const InstDesc* insts, long long NP, const T* exc, const int* h,
+                               TileQueue q, unsigned long long* cnt, unsigned* hmx) {
+  __shared__ unsigned s_max[32];
+  __shared__ unsigned long long s_cnt[32];
+  const InstDesc& I = insts[0];
+  const bool on = !I.done && I.active;
+  const Geo& g = I.g;
+  unsigned hv = 0, na = 0;
+  const int lane = threadIdx.x & 31;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; on && i < NP;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int hh = h[i];
+    if (hh < kHInf && (unsigned)hh > hv) hv = (unsigned)hh;
+    const bool a = exc[i] > 0 && hh < kHInf;
+    na += a ? 1u : 0u;
+    if (__ballot_sync(0xffffffffu, a) && lane == 0) {
+      const int c = int(i % g.Cp);
+      const long long r = i / g.Cp;
+      enqueue_tile(q, 0, I.tile_base + tile_of(g, int(r / g.Bp), int(r % g.Bp), c));
+    }
+  }
+  hv = __reduce_max_sync(0xffffffffu, hv);
+  na = __reduce_add_sync(0xffffffffu, na);
+  if (lane == 0) {
+    s_max[threadIdx.x >> 5] = hv;
+    s_cnt[threadIdx.x >> 5] = na;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const bool w = threadIdx.x < (blockDim.x >> 5);
+    unsigned m = w ? s_max[threadIdx.x] : 0u;
+    unsigned long long c = w ? s_cnt[threadIdx.x] : 0ull;
+    m = __reduce_max_sync(0xffffffffu, m);
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if (threadIdx.x == 0) {
+      if (m) atomicMax(hmx, m);
+      if (c) atomicAdd(cnt, c);
+    }
   }
 }
 
@@ -357,12 +403,12 @@ void PoolRunner::setup(const std::vector<InstDesc>& insts, cudaStream_t s) {
   check(cudaMalloc(&d_hmx, std::max(n, 1) * sizeof(unsigned)), "cudaMalloc");
   check(cudaMalloc(&d_sum, 2 * std::max(n, 1) * sizeof(long long)), "cudaMalloc");
   check(cudaMalloc(&d_flag, sizeof(int)), "cudaMalloc");
-  check(cudaMalloc(&d_counters, 4 * sizeof(unsigned long long)), "cudaMalloc");
+  check(cudaMalloc(&d_counters, 8 * sizeof(unsigned long long)), "cudaMalloc");
   check(cudaMallocHost(&h_pin, 4096), "cudaMallocHost");
   check(cudaMemcpyAsync(d_inst, host.data(), n * sizeof(InstDesc), cudaMemcpyHostToDevice, stream), "memcpy");
   check(cudaMemcpyAsync(d_nbase, nb.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, stream), "memcpy");
   check(cudaMemcpyAsync(d_tile_inst, ti.data(), T * sizeof(int), cudaMemcpyHostToDevice, stream), "memcpy");
-  check(cudaMemsetAsync(d_counters, 0, 4 * sizeof(unsigned long long), stream), "memset");
+  check(cudaMemsetAsync(d_counters, 0, 8 * sizeof(unsigned long long), stream), "memset");
   check(cudaStreamSynchronize(stream), "sync");
   // kernel sizes of the pool (at most two distinct) and launch shapes
   ka = kb = 0;
@@ -423,6 +469,7 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
   const int grid = std::max(tiles, 1);
   const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
   const long long cap = 4LL * tiles + 64;
+  const int k2d = tune.bfs_kernel != 1 ? lattice2d_kernel_size(host[0], n == 1) : 0;
   int cur = 0;
   for (long long pass = 0;;) {
     if (pass > cap) throw LfError{4, "global relabel did not converge"};
@@ -431,7 +478,8 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
       check(cudaMemsetAsync(d_flag, 0, sizeof(int), stream), "memset");
       PoolBFS p{host[0], d_inst, d_tile_inst, h, mask, q, cur, 64, d_flag, d_counters};
       mark(1, false);
-      check(launch_pool_bfs(p, ka, kb, n == 1, grid, threads, smem, stream), "bfs pass");
+      if (k2d) check(launch_pool_bfs2d(p, k2d, d_counters + 4, grid, stream), "bfs pass (TMA)");
+      else check(launch_pool_bfs(p, ka, kb, n == 1, grid, threads, smem, stream), "bfs pass");
       check(cudaGetLastError(), "bfs pass");
       mark(1, true);
       count_launch();
@@ -451,7 +499,11 @@ unsigned long long PoolRunner::activate(const T* exc, const int* h) {
   check(cudaMemsetAsync(d_cnt, 0, n * sizeof(unsigned long long), stream), "memset");
   check(cudaMemsetAsync(d_hmx, 0, n * sizeof(unsigned), stream), "memset");
   check(cudaMemsetAsync(d_counters + 3, 0, sizeof(unsigned long long), stream), "memset");
-  k_pool_active<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, exc, h, q, d_cnt, d_hmx);
+  if (n == 1)  // NP is a whole number of 32-node tile rows
+    k_pool_active1<T><<<std::min(nblk(NP, B), 152 * 8), B, 0, stream>>>(d_inst, NP, exc, h, q,
+                                                                        d_cnt, d_hmx);
+  else
+    k_pool_active<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, exc, h, q, d_cnt, d_hmx);
   count_launch();
   const long long hcap = (long long)kHInf - 2;
   const int slack = tune.height_slack > 0 ? tune.height_slack : 16;
@@ -459,9 +511,18 @@ unsigned long long PoolRunner::activate(const T* exc, const int* h) {
   count_launch();
   check(cudaGetLastError(), "activate");
   unsigned long long total = 0;
-  sync_read(&total, d_counters + 3, sizeof(total));
-  // a pool of one passes its descriptor by value: refresh cap / finished flag
-  if (n == 1) sync_read(&host[0], d_inst, sizeof(InstDesc));
+  if (n == 1) {
+    // a pool of one passes its descriptor by value: refresh cap / finished
+    // flag, in the same synchronisation as the count
+    unsigned char* hp = static_cast<unsigned char*>(h_pin);
+    check(cudaMemcpyAsync(hp, d_counters + 3, sizeof(total), cudaMemcpyDeviceToHost, stream), "memcpy");
+    check(cudaMemcpyAsync(hp + 64, d_inst, sizeof(InstDesc), cudaMemcpyDeviceToHost, stream), "memcpy");
+    check(cudaStreamSynchronize(stream), "sync");
+    std::memcpy(&total, hp, sizeof(total));
+    std::memcpy(&host[0], hp + 64, sizeof(InstDesc));
+  } else {
+    sync_read(&total, d_counters + 3, sizeof(total));
+  }
   return total;
 }
 
@@ -473,6 +534,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   count_launch();
   for (InstDesc& I : host) I.done = 0;
   check(cudaMemsetAsync(d_counters, 0, 3 * sizeof(unsigned long long), stream), "memset");
+  check(cudaMemsetAsync(d_counters + 4, 0, sizeof(unsigned long long), stream), "memset");
   const int M = tune.launches_per_relabel > 0 ? tune.launches_per_relabel : 4;
   const int R = tune.sweeps > 0 ? tune.sweeps : 4;
   const int KA = ka, KB = kb;
@@ -529,8 +591,18 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
       prep_pass(cur);
       PoolPR<T> p{host[0], d_inst, d_tile_inst, res, exc, h, kmask, q, cur, R, d_counters};
       mark(0, false);
-      check(launch_pool_pr<T>(p, KA, KB, NTmax, smem, n == 1, std::max(tiles, 1), stream),
-            "push-relabel pass");
+      int k2d = 0;
+      if constexpr (std::is_same<T, int>::value)
+        if (tune.pr_kernel != 1) k2d = pr2d_kernel_size(p, n == 1);
+      if (k2d) {
+        if constexpr (std::is_same<T, int>::value)
+          check(launch_pool_pr2d(p, k2d, tune.pr_kernel == 2 ? 32 : 40, d_counters + 4,
+                                 std::max(tiles, 1), stream),
+                "push-relabel pass (TMA)");
+      } else {
+        check(launch_pool_pr<T>(p, KA, KB, NTmax, smem, n == 1, std::max(tiles, 1), stream),
+              "push-relabel pass");
+      }
       mark(0, true);
       count_launch();
       ++stats.pr_launches;
@@ -539,10 +611,11 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
     drain_queue();
   }
   if (sets) reach<T>(exc, mask, markv, stats);
-  unsigned long long c[2];
+  unsigned long long c[5];
   sync_read(c, d_counters, sizeof(c));
   stats.tiles_processed += c[0];
   stats.bfs_tiles += c[1];
+  if (c[4]) throw LfError{6, "a tile's staging copy did not complete in time"};
 }
 
 template <typename T>

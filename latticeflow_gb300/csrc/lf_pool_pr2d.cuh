@@ -1,0 +1,313 @@
+// Push/relabel tile pass specialised for one 2-d lattice with a 3x3
+// neighbourhood (Full2d_4, Full2d_8) and 32-bit capacities, tiles staged
+// into shared memory by TMA.
+//
+// Same algorithm as pr_tile (lf_pool_tile.cuh): up to `sweeps` rounds of a
+// push phase with frozen heights and a relabel phase per tile visit, pushes
+// across the tile edge delivered at once with global atomics.  What differs
+// is how the work maps onto the SM:
+//   * the stencil is a compile-time table (offsets become immediates in the
+//     shared-memory addresses, the tile-edge tests fold to a few predicates);
+//   * one elected thread stages a visit's tile with three bulk tensor copies
+//     (cp.async.bulk.tensor): every residual plane as one 3-d box
+//     {32 x TB x K}, the excess as a 2-d box {32 x TB}, the heights with
+//     their one-node halo as a 2-d box {40 x (TB + 2)} starting at column
+//     c0 - 4 (the innermost coordinate stays a multiple of 16 bytes; the
+//     copy's zero fill stands in for nodes outside the lattice, whose
+//     heights are never read because no residual leads there);
+//   * two stage buffers: while the CTA works on one tile, the copies of the
+//     next tile it will take from the queue are already in flight.
+// A prefetched tile can only be staler than one loaded at the start of its
+// visit, and staleness is safe: its excess and its residuals across the
+// tile edge only grow through other tiles' pushes (the visit writes those
+// back as deltas), and its interior belongs to this visit alone (a tile sits
+// at most once in a pass's list).
+//
+// Every wait on a copy is bounded; a CTA whose copies do not land in time
+// records the fault (the host turns it into an error) and returns once its
+// copies have landed or a second bound has passed.
+#pragma once
+
+#include <cuda.h>
+
+#include "lf_pool.cuh"
+#include "lf_tile_common.cuh"
+
+namespace lfg {
+
+// Compile-time 2-d stencils, lattice order of the kernel registry: the
+// positive half first, entry k + K/2 the reverse of entry k.  Each row /
+// column offset (-1, 0, 1) is stored as offset + 1 in two bits.
+template <int K> struct Stencil2d;
+template <> struct Stencil2d<4> {  // (0,1) (1,0) (0,-1) (-1,0)
+  static constexpr unsigned kDB = (1u << 0) | (2u << 2) | (1u << 4) | (0u << 6);
+  static constexpr unsigned kDC = (2u << 0) | (1u << 2) | (0u << 4) | (1u << 6);
+};
+template <> struct Stencil2d<8> {  // (0,1) (1,-1) (1,0) (1,1) (0,-1) (-1,1) (-1,0) (-1,-1)
+  static constexpr unsigned kDB = (1u << 0) | (2u << 2) | (2u << 4) | (2u << 6) |
+                                  (1u << 8) | (0u << 10) | (0u << 12) | (0u << 14);
+  static constexpr unsigned kDC = (2u << 0) | (0u << 2) | (1u << 4) | (2u << 6) |
+                                  (0u << 8) | (2u << 10) | (1u << 12) | (0u << 14);
+};
+template <int K> __host__ __device__ constexpr int s2_db(int k) {
+  return int((Stencil2d<K>::kDB >> (2 * k)) & 3u) - 1;
+}
+template <int K> __host__ __device__ constexpr int s2_dc(int k) {
+  return int((Stencil2d<K>::kDC >> (2 * k)) & 3u) - 1;
+}
+
+constexpr int kPr2dHaloW = 40;  // staged height row: columns c0-4 .. c0+35
+
+// tensor maps of one lattice's residual planes, excess and heights
+struct PR2dMaps {
+  CUtensorMap res;
+  CUtensorMap exc;
+  CUtensorMap h;
+};
+
+template <int K, int TB>
+struct PR2dLayout {
+  static constexpr int NT = TB * 32;
+  static constexpr int HR = TB + 2;
+  static constexpr int res_bytes = K * NT * 4;
+  static constexpr int exc_bytes = NT * 4;
+  static constexpr int h_bytes = HR * kPr2dHaloW * 4;
+  static constexpr int stage_bytes = (res_bytes + exc_bytes + h_bytes + 127) / 128 * 128;
+  static constexpr int tx_bytes = res_bytes + exc_bytes + h_bytes;
+  // two stage buffers, two mbarriers, alignment slack
+  static constexpr int smem_bytes = 2 * stage_bytes + 16 + 128;
+};
+
+// ------------------------------------------------------------ PTX helpers
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait for the phase with the given parity to complete
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity, int limit) {
+  for (int i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap* map, int x, int y,
+                                            unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap* map, int x, int y,
+                                            int z, unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+// ------------------------------------------------------------ the pass
+
+constexpr int kPr2dWaitLimit = 1 << 20;  // try_wait rounds before a copy counts as lost
+
+template <int K, int TB>
+__device__ __forceinline__ void pr2d_issue(const PR2dMaps& maps, const Geo& g, int tile,
+                                           unsigned stage, unsigned bar) {
+  using Ly = PR2dLayout<K, TB>;
+  const int tc = tile % g.ntc, tb = tile / g.ntc;
+  const int b0 = tb * TB, c0 = tc * 32;
+  mbar_expect_tx(bar, Ly::tx_bytes);
+  tma_load_3d(stage, &maps.res, c0, b0, 0, bar);
+  tma_load_2d(stage + Ly::res_bytes, &maps.exc, c0, b0, bar);
+  tma_load_2d(stage + Ly::res_bytes + Ly::exc_bytes, &maps.h, c0 - 4, b0 - 1, bar);
+}
+
+// e0 / my_h: the node's staged excess and height, read by every thread
+// before the barrier that opens the visit (once a visit runs, neighbours
+// push into s_exc at once, and a later read would miss the flow they sent,
+// which the delta write-back of the excess needs).
+template <int K, int TB>
+__device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const Geo& g, int hmax,
+                                          unsigned char* stage, int tile, const int e0,
+                                          int my_h) {
+  using Ly = PR2dLayout<K, TB>;
+  constexpr int NT = Ly::NT;
+  constexpr int HW = kPr2dHaloW;
+  int* s_res = reinterpret_cast<int*>(stage);
+  int* s_exc = reinterpret_cast<int*>(stage + Ly::res_bytes);
+  int* s_h = reinterpret_cast<int*>(stage + Ly::res_bytes + Ly::exc_bytes);
+  const int t = threadIdx.x;
+  const int ic = t & 31, ib = t >> 5;
+  const int tc = tile % g.ntc, tb = tile / g.ntc;
+  const int b0 = tb * TB, c0 = tc * 32;
+  const long long gi = (long long)(b0 + ib) * g.Cp + (c0 + ic);
+  const int hidx = (ib + 1) * HW + (ic + 4);
+  const int nxt = p.cur ^ 1;
+  // directions that leave the tile
+  unsigned outm = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int nb = ib + s2_db<K>(k), nc = ic + s2_dc<K>(k);
+    if (nb < 0 || nb >= TB || nc < 0 || nc >= 32) outm |= 1u << k;
+  }
+  for (int it = 0; it < p.sweeps; ++it) {
+    int e = s_exc[t];
+    // a node parked at the epoch cap no longer relabels but still pushes
+    // downhill (a lower neighbour may be a deficit)
+    if (e > 0) {
+      int sent = 0;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int rem = e - sent;
+        if (rem <= 0) break;
+        const int r = s_res[k * NT + t];
+        if (r <= 0) continue;
+        if (s_h[hidx + s2_db<K>(k) * HW + s2_dc<K>(k)] >= my_h) continue;
+        const int d = rem < r ? rem : r;
+        s_res[k * NT + t] = r - d;
+        sent += d;
+        constexpr int half = K / 2;
+        const int rk = k < half ? k + half : k - half;
+        if (!((outm >> k) & 1u)) {
+          const int tn = t + s2_db<K>(k) * 32 + s2_dc<K>(k);
+          atomicAdd(&s_exc[tn], d);
+          s_res[rk * NT + tn] += d;
+        } else {
+          // across the tile edge: delivered at once with global atomics
+          int* r0 = p.res + gi;
+          atomicAdd(r0 + (long long)k * g.NP, -d);
+          const long long dn = (long long)s2_db<K>(k) * g.Cp + s2_dc<K>(k);
+          atomicAdd(r0 + (long long)rk * g.NP + dn, d);
+          atomicAdd(p.exc + gi + dn, d);
+          // the neighbour's tile: one tile row / column over where the
+          // neighbour leaves this tile's rows / columns
+          const int dtb = (s2_db<K>(k) < 0 && ib == 0) ? -1 : (s2_db<K>(k) > 0 && ib == TB - 1) ? 1 : 0;
+          const int dtc = (s2_dc<K>(k) < 0 && ic == 0) ? -1 : (s2_dc<K>(k) > 0 && ic == 31) ? 1 : 0;
+          enqueue_tile(p.q, nxt, tile + dtb * g.ntc + dtc);
+        }
+      }
+      if (sent) atomicAdd(&s_exc[t], -sent);
+    }
+    __syncthreads();
+    e = s_exc[t];
+    int act = 0;
+    if (e > 0 && my_h < hmax) {
+      int hmin = kHInf;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        if (s_res[k * NT + t] > 0) {
+          const int hn = s_h[hidx + s2_db<K>(k) * HW + s2_dc<K>(k)];
+          hmin = hn < hmin ? hn : hmin;
+        }
+      }
+      if (hmin >= my_h) {
+        my_h = (hmin >= hmax - 1) ? hmax : hmin + 1;
+        s_h[hidx] = my_h;
+      }
+      act = my_h < hmax;
+    }
+    if (!__syncthreads_or(act)) break;
+  }
+  __syncthreads();
+  const int ef = s_exc[t];
+  if (outm) atomicAdd(&p.exc[gi], ef - e0);
+  else p.exc[gi] = ef;
+#pragma unroll
+  for (int k = 0; k < K; ++k)  // edges across the tile edge were updated by their pushes
+    if (!((outm >> k) & 1u)) p.res[(long long)k * g.NP + gi] = s_res[k * NT + t];
+  p.h[gi] = my_h;
+  // the buffer's next contents come from the async proxy: order this
+  // visit's shared-memory accesses before them
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  const int still = ef > 0 && my_h < hmax;
+  if (__syncthreads_or(still) && t == 0) enqueue_tile(p.q, nxt, tile);
+}
+
+// One lattice (the pool of one), no section mask, 32-bit capacities.
+// `fault` (global) records a copy that did not land in time.  REGS caps the
+// registers per thread: 40 keeps three 512-thread tiles on an SM without
+// spills, 32 fits four (with a few spilled values for 8 directions).
+template <int K, int TB, int REGS>
+__global__ void __maxnreg__(REGS)
+    k_pool_pr2d(const __grid_constant__ PR2dMaps maps, PoolPR<int> p,
+                unsigned long long* fault) {
+  using Ly = PR2dLayout<K, TB>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<unsigned long long>(smem_raw) + 127) & ~127ull);
+  const unsigned bar0 = smem_addr(smem + 2 * Ly::stage_bytes);  // two mbarriers, 8 bytes apart
+  const unsigned stage0 = smem_addr(smem);
+  const Geo& g = p.inst0.g;
+  const int hmax = p.inst0.hmax;
+  const unsigned n = queued_count(p.q, p.cur);
+  const int* list = p.q.list[p.cur];
+  if (blockIdx.x >= n) return;
+  if (threadIdx.x == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar0 + 8, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const bool done = p.inst0.done != 0;
+  if (threadIdx.x == 0 && !done) pr2d_issue<K, TB>(maps, g, list[blockIdx.x], stage0, bar0);
+  unsigned phases = 0;  // bit b: parity of the next phase of buffer b
+  unsigned buf = 0;
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x, buf ^= 1) {
+    const int gt = list[i];
+    if (threadIdx.x == 0) {
+      p.q.flag[p.cur][gt] = 0;
+      atomicAdd(&p.counters[0], 1ull);
+    }
+    if (done) continue;
+    // the next tile of this CTA: its copies fly while this one is worked on
+    // (the other buffer was released by the barrier that ended its visit)
+    const unsigned nx = i + gridDim.x;
+    if (threadIdx.x == 0 && nx < n)
+      pr2d_issue<K, TB>(maps, g, list[nx], stage0 + (buf ^ 1) * Ly::stage_bytes,
+                        bar0 + (buf ^ 1) * 8);
+    const unsigned bar = bar0 + buf * 8;
+    const unsigned par = (phases >> buf) & 1u;
+    const bool ok = mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+    phases ^= 1u << buf;
+    // this node's excess and height as staged (see pr2d_tile)
+    unsigned char* st = smem + buf * Ly::stage_bytes;
+    const int e0 = reinterpret_cast<const int*>(st + Ly::res_bytes)[threadIdx.x];
+    const int h0 = reinterpret_cast<const int*>(st + Ly::res_bytes + Ly::exc_bytes)
+        [((threadIdx.x >> 5) + 1) * kPr2dHaloW + (threadIdx.x & 31) + 4];
+    if (__syncthreads_or(!ok)) {
+      // a copy did not land: record it, wait (bounded) for the copies still
+      // in flight so that none lands after the CTA is gone, and stop
+      if (threadIdx.x == 0) atomicExch(fault, 1ull);
+      mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+      if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
+      return;
+    }
+    pr2d_tile<K, TB>(p, g, hmax, st, gt, e0, h0);
+  }
+}
+
+}  // namespace lfg

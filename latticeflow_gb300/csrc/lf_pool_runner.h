@@ -24,6 +24,11 @@ struct Tuning {
   int tail_active = 0;           // active nodes at most for the tail step; 0 = 64, < 0 = off
   int max_epochs = 0;            // global relabels per solve at most; 0 = 1,000,000
   int tail_tree_nodes = 0;       // nodes of one tail-step tree at most; 0 = 65,536
+  int pr_kernel = 0;             // push/relabel pass of a plain 2-d cut: 0 = TMA-staged
+                                 // (40 registers), 1 = generic tile kernel, 2 = TMA-staged
+                                 // with 32 registers
+  int bfs_kernel = 0;            // BFS pass of a single 2-d lattice: 0 = TMA-staged,
+                                 // 1 = generic tile kernel
 };
 
 struct SolveStats {
@@ -71,6 +76,17 @@ size_t pool_pr_smem(int K, int NT, int HV) {
 template <typename T>
 cudaError_t launch_pool_pr(const PoolPR<T>& p, int KA, int KB, int threads, size_t smem,
                            bool single, int grid, cudaStream_t s);
+
+// The TMA-staged 2-d passes (lf_pool_pr2d.cu): the kernel size they take a
+// lattice with (4 or 8), or 0 when it does not fit them (not a pool of one,
+// not a 2-d 3x3 neighbourhood in registry order; the push/relabel pass also
+// takes no section mask).
+int lattice2d_kernel_size(const InstDesc& I, bool single);
+int pr2d_kernel_size(const PoolPR<int>& p, bool single);
+cudaError_t launch_pool_pr2d(const PoolPR<int>& p, int K, int regs, unsigned long long* fault,
+                             int tiles, cudaStream_t s);
+cudaError_t launch_pool_bfs2d(const PoolBFS& p, int K, unsigned long long* fault, int tiles,
+                              cudaStream_t s);
 
 cudaError_t launch_pool_bfs(const PoolBFS& p, int KA, int KB, bool single, int grid, int threads,
                             size_t smem, cudaStream_t s);
@@ -140,7 +156,8 @@ class PoolRunner {
   unsigned* d_hmx = nullptr;
   long long* d_sum = nullptr;
   int* d_flag = nullptr;
-  unsigned long long* d_counters = nullptr;  // [0] pr tiles, [1] bfs tiles, [3] active total
+  unsigned long long* d_counters = nullptr;  // [0] pr tiles, [1] bfs tiles, [2] tail moved,
+                                             // [3] active total, [4] staging fault
   void* h_pin = nullptr;
   int threads = 1, hv_max = 0;
   int ka = 0, kb = 0;  // kernel sizes present in the pool

@@ -222,3 +222,74 @@ def test_pinned_host_arrays_read_in_place(native, gpu):
     e.addCapacities(p.source, p.sink, p.edge)
     e.run()
     assert d.flow() == e.flow() and np.array_equal(d.getCut(), e.getCut())
+
+
+@pytest.mark.parametrize("pr_kernel,bfs_kernel", [(0, 0), (1, 1), (2, 0), (1, 0), (0, 1)])
+@pytest.mark.parametrize("kernel,dims,tile_rows", [
+    ("Full2d_8", (200, 230), 8), ("Full2d_8", (256, 160), 16), ("Full2d_8", (97, 300), 32),
+    ("Full2d_4", (210, 190), 16), ("Full2d_4", (64, 500), 32)], ids=lambda v: str(v))
+def test_push_relabel_kernels_agree(native, gpu, oracle_port, pr_kernel, bfs_kernel, kernel, dims,
+                                    tile_rows):
+    """The TMA-staged 2-d passes (pr_kernel 0, 2; bfs_kernel 0) and the
+    generic tile passes (1) give the reference's exact answer at every tile
+    height."""
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    p = W.plain_cut(30 + tile_rows, dims, kernel)
+    u, b = p.energies()
+    E, cmin, cmax, _, _ = oracle_port.port_canonical(p.kernel, p.dims, u, b)
+    L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    L.setParam("pr_kernel", pr_kernel)
+    L.setParam("bfs_kernel", bfs_kernel)
+    L.setTuning(tile_rows=tile_rows, local_sweeps=3, launches_per_relabel=4)
+    L.addEnergyPotentials(u, b)
+    L.run()
+    assert L.layout()[0] == (1, tile_rows, 32)
+    assert L.flow()[1] == E
+    assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
+
+
+@pytest.mark.parametrize("pr_kernel", [0, 2])
+def test_tma_pass_large_cut_scaled(native, gpu, oracle_port, pr_kernel):
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    p = W.large_cut(1, n=512)
+    u, b = p.energies()
+    E, cmin, cmax, _, _ = oracle_port.port_canonical(p.kernel, p.dims, u, b)
+    L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    L.setParam("pr_kernel", pr_kernel)
+    L.addEnergyPotentials(u, b)
+    L.run()
+    assert L.flow()[1] == E
+    assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
+
+
+def test_tma_pass_full_size_all_variants(native, gpu, oracle_port):
+    """2048x2048 Full2d_8 at full size through every push/relabel variant and
+    tile height: the same flow value, both cut sets identical, each set's
+    energy equal to the reported minimum (a pass that loses flow at a tile
+    edge shows up here as a larger flow than the cut's energy)."""
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    p = W.large_cut(0)
+    u, b = p.energies()
+    ref = None
+    for prk, rows in ((1, 16), (0, 16), (2, 16), (0, 8), (2, 8), (0, 32), (2, 32)):
+        L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+        L.setParam("pr_kernel", prk)
+        L.setParam("bfs_kernel", 1 if ref is None else 0)  # the reference run: generic passes
+        L.setTuning(tile_rows=rows, local_sweeps=2, launches_per_relabel=8)
+        for _ in range(2):
+            L.clear()
+            L.addEnergyPotentials(u, b)
+            L.run()
+            flow, energy = L.flow()
+            cmin, cmax = L.getCut(), L.getCutMax()
+            if ref is None:
+                assert flow == energy
+                assert oracle_port.energy(p.kernel, p.dims, u, b, cmin) == energy
+                assert oracle_port.energy(p.kernel, p.dims, u, b, cmax) == energy
+                ref = (flow, energy, cmin.copy(), cmax.copy())
+            assert (flow, energy) == ref[:2], (prk, rows)
+            assert np.array_equal(cmin, ref[2]) and np.array_equal(cmax, ref[3]), (prk, rows)
+        del L
