@@ -257,7 +257,7 @@ void Engine::add_caps(const int32_t* src, const int32_t* snk, const int32_t* edg
 
 // Working arrays in the chosen capacity type, converted from the int64
 // accumulators, and the pool runner for this single lattice.
-void Engine::prepare_working(int elem) {
+void Engine::prepare_working(int elem, bool convert) {
   if (elem != elem_bytes) {
     free_working();
     elem_bytes = elem;
@@ -310,6 +310,7 @@ void Engine::prepare_working(int elem) {
     runner.setup(insts, stream);
     runner_ready = true;
   }
+  if (!convert) return;
   if (elem == 4) {
     check(counted(launch_convert<int>((long long)st.K * g.NP, d_cap64, (int*)d_res, stream)), "convert");
     check(counted(launch_convert<int>(g.NP, d_exc64, (int*)d_exc, stream)), "convert");
@@ -337,14 +338,27 @@ void Engine::run() {
   for (int i = 0; i < 4; ++i) prof_ms[i] = 0;
   for (int i = 0; i < 6; ++i) prof_cnt[i] = 0;
   pev_used = 0;
-  // choose 32-bit working arrays when every reachable value fits
-  check(cudaMemsetAsync(d_u64 + 1, 0, sizeof(unsigned long long), stream), "memset");
-  check(counted(launch_range_bound(g, st, d_exc64, d_cap64, d_u64 + 1, stream)), "range bound");
-  unsigned long long bound = 0;
-  sync_read(&bound, d_u64 + 1, sizeof(bound));
-  if (bound >= (1ULL << 62)) throw LfError{3, "capacities exceed the 63-bit range"};
-  int elem = bound < (unsigned long long)INT_MAX ? 4 : 8;
-  prepare_working(elem);
+  // choose 32-bit working arrays when every reachable value fits: first
+  // the 32-bit copies with a loose bound in one pass; only when that bound
+  // fails, the exact per-node bound (and the copies again, or 64-bit arrays)
+  prepare_working(4, false);
+  check(cudaMemsetAsync(d_u64 + 2, 0, 2 * sizeof(unsigned long long), stream), "memset");
+  check(counted(launch_convert_bounded(g.NP, st.K, d_exc64, d_cap64, (int*)d_exc, (int*)d_res,
+                                       d_u64 + 2, stream)), "convert");
+  unsigned long long mx[2] = {0, 0};
+  sync_read(mx, d_u64 + 2, sizeof(mx));
+  const unsigned long long lim = (unsigned long long)INT_MAX;
+  const bool loose_ok = mx[0] < lim && mx[1] < lim &&
+                        mx[0] + 2ULL * (unsigned long long)st.K * mx[1] < lim;
+  if (!loose_ok) {
+    check(cudaMemsetAsync(d_u64 + 1, 0, sizeof(unsigned long long), stream), "memset");
+    check(counted(launch_range_bound(g, st, d_exc64, d_cap64, d_u64 + 1, stream)), "range bound");
+    unsigned long long bound = 0;
+    sync_read(&bound, d_u64 + 1, sizeof(bound));
+    if (bound >= (1ULL << 62)) throw LfError{3, "capacities exceed the 63-bit range"};
+    prepare_working(bound < lim ? 4 : 8);
+  }
+  const int elem = elem_bytes;
   check(cudaMemsetAsync(d_sum, 0, 4 * sizeof(long long), stream), "memset");
   check(cudaEventRecord(ev0, stream), "event");
   if (elem == 4) {

@@ -28,6 +28,9 @@ cudaError_t launch_range_bound(const Geo& g, const Stencil& st, const long long*
                                const long long* cap, unsigned long long* out, cudaStream_t s);
 template <typename T>
 cudaError_t launch_convert(long long n, const long long* src, T* dst, cudaStream_t s);
+cudaError_t launch_convert_bounded(long long NP, int K, const long long* exc64,
+                                  const long long* cap64, int* exc, int* res,
+                                  unsigned long long* mx, cudaStream_t s);
 template <typename T>
 cudaError_t launch_sum_pos(long long n, const T* x, long long* out, cudaStream_t s);
 cudaError_t launch_extract_cuts(const Geo& g, int nd, long long N, const int* mark, const int* h,
@@ -101,7 +104,7 @@ class Engine : public ProfHooks {
 
   void choose_geometry(int elem);
   void alloc_accumulators();
-  void prepare_working(int elem);
+  void prepare_working(int elem, bool convert = true);
   template <typename T> void maxflow(bool compute_sets);
   void sync_read(void* host, const void* dev, size_t bytes);
   void check(cudaError_t e, const char* what) const;

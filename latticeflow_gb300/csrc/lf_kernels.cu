@@ -146,6 +146,49 @@ __global__ void k_range_bound(Geo g, Stencil st, const long long* exc, const lon
   if ((threadIdx.x & 31) == 0 && m) atomicMax(out_max, m);
 }
 
+// 32-bit working arrays written at once, with a looser range bound than
+// k_range_bound: |exc| <= mx_exc and every capacity <= mx_cap give any
+// node's excess or residual at most mx_exc + 2 K mx_cap.  When that bound
+// stays below 2^31 the copies are the working arrays; otherwise the exact
+// per-node bound decides (and the copies are discarded or redone).
+__global__ void k_convert_bounded(long long NP, int K, const long long* exc64,
+                                  const long long* cap64, int* exc, int* res,
+                                  unsigned long long* mx /* [0] |exc|, [1] cap */) {
+  __shared__ unsigned long long s_e[32], s_c[32];
+  unsigned long long me = 0, mc = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < NP;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long e = exc64[i];
+    const unsigned long long ae = (unsigned long long)(e < 0 ? -e : e);
+    me = ae > me ? ae : me;
+    exc[i] = (int)e;
+    for (int k = 0; k < K; ++k) {
+      const long long c = cap64[(long long)k * NP + i];
+      mc = (unsigned long long)c > mc ? (unsigned long long)c : mc;
+      res[(long long)k * NP + i] = (int)c;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long xe = __shfl_down_sync(0xffffffffu, me, o);
+    const unsigned long long xc = __shfl_down_sync(0xffffffffu, mc, o);
+    me = xe > me ? xe : me;
+    mc = xc > mc ? xc : mc;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_e[threadIdx.x >> 5] = me;
+    s_c[threadIdx.x >> 5] = mc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < int(blockDim.x >> 5); ++w) {
+      me = s_e[w] > me ? s_e[w] : me;
+      mc = s_c[w] > mc ? s_c[w] : mc;
+    }
+    if (me) atomicMax(&mx[0], me);
+    if (mc) atomicMax(&mx[1], mc);
+  }
+}
+
 template <typename T>
 __global__ void k_convert(long long n, const long long* src, T* dst) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -219,6 +262,15 @@ cudaError_t launch_fill_caps(const Geo& g, const Stencil& st, int nd, long long 
 cudaError_t launch_range_bound(const Geo& g, const Stencil& st, const long long* exc,
                                const long long* cap, unsigned long long* out, cudaStream_t s) {
   k_range_bound<<<nblk(g.NP, 256), 256, 0, s>>>(g, st, exc, cap, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_convert_bounded(long long NP, int K, const long long* exc64,
+                                  const long long* cap64, int* exc, int* res,
+                                  unsigned long long* mx, cudaStream_t s) {
+  if (NP > 0)
+    k_convert_bounded<<<std::min(nblk(NP, 256), 152 * 8), 256, 0, s>>>(NP, K, exc64, cap64, exc,
+                                                                       res, mx);
   return cudaGetLastError();
 }
 

@@ -326,6 +326,10 @@ void PoolRunner::release() {
   cudaFree(d_sum); d_sum = nullptr;
   cudaFree(d_flag); d_flag = nullptr;
   cudaFree(d_counters); d_counters = nullptr;
+  cudaFree(d_ctl); d_ctl = nullptr;
+  if (loop_pr) pass_loop_free(loop_pr);
+  if (loop_bfs) pass_loop_free(loop_bfs);
+  loop_pr = loop_bfs = nullptr;
   if (h_pin) { cudaFreeHost(h_pin); h_pin = nullptr; }
   free_tail();
 }
@@ -403,12 +407,13 @@ void PoolRunner::setup(const std::vector<InstDesc>& insts, cudaStream_t s) {
   check(cudaMalloc(&d_hmx, std::max(n, 1) * sizeof(unsigned)), "cudaMalloc");
   check(cudaMalloc(&d_sum, 2 * std::max(n, 1) * sizeof(long long)), "cudaMalloc");
   check(cudaMalloc(&d_flag, sizeof(int)), "cudaMalloc");
-  check(cudaMalloc(&d_counters, 8 * sizeof(unsigned long long)), "cudaMalloc");
+  check(cudaMalloc(&d_counters, 16 * sizeof(unsigned long long)), "cudaMalloc");
+  check(cudaMalloc(&d_ctl, 4 * sizeof(int)), "cudaMalloc");
   check(cudaMallocHost(&h_pin, 4096), "cudaMallocHost");
   check(cudaMemcpyAsync(d_inst, host.data(), n * sizeof(InstDesc), cudaMemcpyHostToDevice, stream), "memcpy");
   check(cudaMemcpyAsync(d_nbase, nb.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, stream), "memcpy");
   check(cudaMemcpyAsync(d_tile_inst, ti.data(), T * sizeof(int), cudaMemcpyHostToDevice, stream), "memcpy");
-  check(cudaMemsetAsync(d_counters, 0, 8 * sizeof(unsigned long long), stream), "memset");
+  check(cudaMemsetAsync(d_counters, 0, 16 * sizeof(unsigned long long), stream), "memset");
   check(cudaStreamSynchronize(stream), "sync");
   // kernel sizes of the pool (at most two distinct) and launch shapes
   ka = kb = 0;
@@ -470,6 +475,19 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
   const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
   const long long cap = 4LL * tiles + 64;
   const int k2d = tune.bfs_kernel != 1 ? lattice2d_kernel_size(host[0], n == 1) : 0;
+  if (k2d && tune.host_loops != 1) {
+    // the whole relabel in one device-side loop: passes until no tile is
+    // queued (a cap that ends it early is reported by activate())
+    if (!loop_bfs) loop_bfs = pass_loop_new();
+    PoolBFS p{host[0], d_inst, d_tile_inst, h, mask, q, 0, 64, d_flag, d_counters};
+    mark(1, false);
+    check(loop_pool_bfs2d(loop_bfs, p, k2d, d_counters + 4, grid, d_ctl, (unsigned)cap,
+                          d_counters + 5, d_counters + 7, stream),
+          "bfs loop (TMA)");
+    mark(1, true);
+    count_launch();
+    return;
+  }
   int cur = 0;
   for (long long pass = 0;;) {
     if (pass > cap) throw LfError{4, "global relabel did not converge"};
@@ -513,13 +531,18 @@ unsigned long long PoolRunner::activate(const T* exc, const int* h) {
   unsigned long long total = 0;
   if (n == 1) {
     // a pool of one passes its descriptor by value: refresh cap / finished
-    // flag, in the same synchronisation as the count
+    // flag, in the same synchronisation as the count (and the cap flag of a
+    // device-side BFS loop, counters[7])
     unsigned char* hp = static_cast<unsigned char*>(h_pin);
-    check(cudaMemcpyAsync(hp, d_counters + 3, sizeof(total), cudaMemcpyDeviceToHost, stream), "memcpy");
+    check(cudaMemcpyAsync(hp, d_counters + 3, 5 * sizeof(total), cudaMemcpyDeviceToHost, stream),
+          "memcpy");
     check(cudaMemcpyAsync(hp + 64, d_inst, sizeof(InstDesc), cudaMemcpyDeviceToHost, stream), "memcpy");
     check(cudaStreamSynchronize(stream), "sync");
-    std::memcpy(&total, hp, sizeof(total));
+    unsigned long long c[5];
+    std::memcpy(c, hp, sizeof(c));
     std::memcpy(&host[0], hp + 64, sizeof(InstDesc));
+    if (c[4]) throw LfError{4, "global relabel did not converge"};
+    total = c[0];
   } else {
     sync_read(&total, d_counters + 3, sizeof(total));
   }
@@ -534,7 +557,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   count_launch();
   for (InstDesc& I : host) I.done = 0;
   check(cudaMemsetAsync(d_counters, 0, 3 * sizeof(unsigned long long), stream), "memset");
-  check(cudaMemsetAsync(d_counters + 4, 0, sizeof(unsigned long long), stream), "memset");
+  check(cudaMemsetAsync(d_counters + 4, 0, 4 * sizeof(unsigned long long), stream), "memset");
   const int M = tune.launches_per_relabel > 0 ? tune.launches_per_relabel : 4;
   const int R = tune.sweeps > 0 ? tune.sweeps : 4;
   const int KA = ka, KB = kb;
@@ -586,6 +609,22 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
         continue;
       }
     }
+    if constexpr (std::is_same<T, int>::value) {
+      PoolPR<int> p{host[0], d_inst, d_tile_inst, res, exc, h, kmask, q, 0, R, d_counters};
+      const int k2d = tune.pr_kernel != 1 ? pr2d_kernel_size(p, n == 1) : 0;
+      if (k2d && tune.host_loops != 1) {
+        // M passes (fewer when the queue runs dry) in one device-side loop
+        if (!loop_pr) loop_pr = pass_loop_new();
+        mark(0, false);
+        check(loop_pool_pr2d(loop_pr, p, k2d, tune.pr_kernel == 2 ? 32 : 40, d_counters + 4,
+                             std::max(tiles, 1), d_ctl, (unsigned)M, d_counters + 6, stream),
+              "push-relabel loop (TMA)");
+        mark(0, true);
+        count_launch();
+        drain_queue();
+        continue;
+      }
+    }
     int cur = 0;
     for (int l = 0; l < M; ++l) {
       prep_pass(cur);
@@ -611,11 +650,14 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
     drain_queue();
   }
   if (sets) reach<T>(exc, mask, markv, stats);
-  unsigned long long c[5];
+  unsigned long long c[8];
   sync_read(c, d_counters, sizeof(c));
   stats.tiles_processed += c[0];
   stats.bfs_tiles += c[1];
+  stats.bfs_passes += (long long)c[5];
+  stats.pr_launches += (long long)c[6];
   if (c[4]) throw LfError{6, "a tile's staging copy did not complete in time"};
+  if (c[7]) throw LfError{4, "global relabel did not converge"};
 }
 
 template <typename T>

@@ -65,9 +65,9 @@ __device__ __forceinline__ unsigned bfs2d_edge_bits(int ib, int ic) {
 }
 
 template <int K, int TB>
-__device__ __forceinline__ void bfs2d_tile(const PoolBFS& p, const Geo& g, unsigned char* stage,
-                                           unsigned* s_flags, int tile, int my_h,
-                                           const uint64_t m) {
+__device__ __forceinline__ void bfs2d_tile(const PoolBFS& p, const Geo& g, int cur,
+                                           unsigned char* stage, unsigned* s_flags, int tile,
+                                           int my_h, const uint64_t m) {
   using Ly = BFS2dLayout<TB>;
   constexpr int HW = kPr2dHaloW;
   int* s_h = reinterpret_cast<int*>(stage);
@@ -76,7 +76,7 @@ __device__ __forceinline__ void bfs2d_tile(const PoolBFS& p, const Geo& g, unsig
   const int tc = tile % g.ntc, tb = tile / g.ntc;
   const long long gi = (long long)(tb * TB + ib) * g.Cp + (tc * 32 + ic);
   const int hidx = (ib + 1) * HW + (ic + 4);
-  const int nxt = p.cur ^ 1;
+  const int nxt = cur ^ 1;
   // the row directions of both stencils: (0, 1) is entry 0, (0, -1) entry K/2
   constexpr int kr = 0, kl = K / 2;
   const bool can_l = (m >> kl) & 1, can_r = (m >> kr) & 1;
@@ -123,10 +123,11 @@ __device__ __forceinline__ void bfs2d_tile(const PoolBFS& p, const Geo& g, unsig
 }
 
 // One lattice (the pool of one).  `fault` records a copy that did not land
-// in time (see k_pool_pr2d).
+// in time; ctl as for k_pool_pr2d.
 template <int K, int TB>
 __global__ void __launch_bounds__(TB * 32, 2048 / (TB * 32))
-    k_pool_bfs2d(const __grid_constant__ BFS2dMaps maps, PoolBFS p, unsigned long long* fault) {
+    k_pool_bfs2d(const __grid_constant__ BFS2dMaps maps, PoolBFS p, unsigned long long* fault,
+                 const int* ctl) {
   using Ly = BFS2dLayout<TB>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
@@ -137,8 +138,9 @@ __global__ void __launch_bounds__(TB * 32, 2048 / (TB * 32))
   unsigned* s_flags = reinterpret_cast<unsigned*>(smem + 2 * Ly::stage_bytes + 16);
   const unsigned stage0 = smem_addr(smem);
   const Geo& g = p.inst0.g;
-  const unsigned n = queued_count(p.q, p.cur);
-  const int* list = p.q.list[p.cur];
+  const int cur = ctl ? *ctl : p.cur;
+  const unsigned n = queued_count(p.q, cur);
+  const int* list = p.q.list[cur];
   if (blockIdx.x >= n) return;
   if (threadIdx.x == 0) {
     mbar_init(bar0, 1);
@@ -146,14 +148,14 @@ __global__ void __launch_bounds__(TB * 32, 2048 / (TB * 32))
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  const bool done = p.inst0.done != 0;
+  const bool done = (ctl ? p.inst[0].done : p.inst0.done) != 0;
   if (threadIdx.x == 0 && !done) bfs2d_issue<TB>(maps, g, list[blockIdx.x], stage0, bar0);
   unsigned phases = 0;
   unsigned buf = 0;
   for (unsigned i = blockIdx.x; i < n; i += gridDim.x, buf ^= 1) {
     const int gt = list[i];
     if (threadIdx.x == 0) {
-      p.q.flag[p.cur][gt] = 0;
+      p.q.flag[cur][gt] = 0;
       atomicAdd(&p.counters[1], 1ull);
       s_flags[buf] = 0;
     }
@@ -175,7 +177,7 @@ __global__ void __launch_bounds__(TB * 32, 2048 / (TB * 32))
       if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
       return;
     }
-    bfs2d_tile<K, TB>(p, g, st, s_flags + buf, gt, h0, m);
+    bfs2d_tile<K, TB>(p, g, cur, st, s_flags + buf, gt, h0, m);
   }
 }
 

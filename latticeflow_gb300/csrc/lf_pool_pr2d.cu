@@ -4,6 +4,8 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdint>
+#include <cstring>
 #include <mutex>
 
 #include "lf_pool_bfs2d.cuh"
@@ -84,24 +86,29 @@ bool maps_for(const PoolPR<int>& p, int K, int TB, PR2dMaps& out) {
 }
 
 template <int K, int TB, int REGS>
-cudaError_t launch_kt(const PR2dMaps& maps, const PoolPR<int>& p, unsigned long long* fault,
-                      int tiles, cudaStream_t s) {
+void* kt_setup(int& grid) {
   using Ly = PR2dLayout<K, TB>;
   auto kern = k_pool_pr2d<K, TB, REGS>;
   static std::mutex mu;
   static int cap = 0;
-  int grid;
-  {
-    std::lock_guard<std::mutex> lk(mu);
-    if (!cap) {
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Ly::smem_bytes);
-      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-      cap = occupancy_grid(kern, Ly::NT, Ly::smem_bytes);
-    }
-    grid = cap;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!cap) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Ly::smem_bytes);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cap = occupancy_grid(kern, Ly::NT, Ly::smem_bytes);
   }
-  kern<<<std::max(1, std::min(grid, tiles)), Ly::NT, Ly::smem_bytes, s>>>(
-      maps, p, fault);
+  grid = cap;
+  return reinterpret_cast<void*>(kern);
+}
+
+template <int K, int TB, int REGS>
+cudaError_t launch_kt(const PR2dMaps& maps, const PoolPR<int>& p, unsigned long long* fault,
+                      int tiles, cudaStream_t s) {
+  using Ly = PR2dLayout<K, TB>;
+  int grid = 0;
+  kt_setup<K, TB, REGS>(grid);
+  k_pool_pr2d<K, TB, REGS><<<std::max(1, std::min(grid, tiles)), Ly::NT, Ly::smem_bytes, s>>>(
+      maps, p, fault, nullptr);
   return cudaGetLastError();
 }
 
@@ -136,24 +143,147 @@ bool bfs_maps_for(const PoolBFS& p, int TB, BFS2dMaps& out) {
 }
 
 template <int K, int TB>
-cudaError_t launch_bfs_kt(const BFS2dMaps& maps, const PoolBFS& p, unsigned long long* fault,
-                          int tiles, cudaStream_t s) {
+void* bfs_kt_setup(int& grid) {
   using Ly = BFS2dLayout<TB>;
   auto kern = k_pool_bfs2d<K, TB>;
   static std::mutex mu;
   static int cap = 0;
-  int grid;
-  {
-    std::lock_guard<std::mutex> lk(mu);
-    if (!cap) {
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Ly::smem_bytes);
-      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-      cap = occupancy_grid(kern, Ly::NT, Ly::smem_bytes);
-    }
-    grid = cap;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!cap) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Ly::smem_bytes);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cap = occupancy_grid(kern, Ly::NT, Ly::smem_bytes);
   }
-  kern<<<std::max(1, std::min(grid, tiles)), Ly::NT, Ly::smem_bytes, s>>>(maps, p, fault);
+  grid = cap;
+  return reinterpret_cast<void*>(kern);
+}
+
+template <int K, int TB>
+cudaError_t launch_bfs_kt(const BFS2dMaps& maps, const PoolBFS& p, unsigned long long* fault,
+                          int tiles, cudaStream_t s) {
+  using Ly = BFS2dLayout<TB>;
+  int grid = 0;
+  bfs_kt_setup<K, TB>(grid);
+  k_pool_bfs2d<K, TB><<<std::max(1, std::min(grid, tiles)), Ly::NT, Ly::smem_bytes, s>>>(
+      maps, p, fault, nullptr);
   return cudaGetLastError();
+}
+
+// ------------------------------------------------------ device-side pass loop
+//
+// A CUDA graph: a memset node zeroes the loop's control words, then a while
+// node runs [pass kernel, k_pass_ctl] until k_pass_ctl finds the list of the
+// next pass empty or the pass cap reached.  k_pass_ctl does between two
+// passes what the host does between two launches (zero the count of the list
+// just consumed, swap the lists) and counts the passes.
+
+// ctl[0]: list the next pass consumes, ctl[1]: passes run in this loop
+__global__ void k_pass_ctl(TileQueue q, int* ctl, unsigned cap, unsigned long long* passes,
+                           unsigned long long* overflow, cudaGraphConditionalHandle h) {
+  const int c = ctl[0], nx = c ^ 1;
+  q.ctr[q_count_idx(c)] = 0;  // consumed; the next pass fills it
+  q.ctr[q_head_idx(nx)] = 0;
+  const unsigned n = q.ctr[q_count_idx(nx)];
+  const unsigned run = (unsigned)ctl[1] + 1;
+  ctl[1] = (int)run;
+  ctl[0] = nx;
+  *passes += 1;
+  if (n > 0 && run >= cap && overflow) *overflow = 1;
+  cudaGraphSetConditional(h, (n > 0 && run < cap) ? 1u : 0u);
+}
+
+}  // namespace
+
+// What a pass loop was built for: it is rebuilt when any of these changes.
+struct PassLoopKey {
+  long long v[32];
+};
+
+struct PassLoop {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  PassLoopKey key{};
+  ~PassLoop() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
+PassLoop* pass_loop_new() { return new PassLoop(); }
+void pass_loop_free(PassLoop* L) { delete L; }
+
+namespace {
+
+cudaError_t run_loop(PassLoop* L, const PassLoopKey& key, void* kern, int grid, int threads,
+                     size_t smem, void** kargs, const TileQueue& q, int* ctl, unsigned cap,
+                     unsigned long long* passes, unsigned long long* overflow, cudaStream_t s) {
+  if (!(L->exec && std::memcmp(&L->key, &key, sizeof(key)) == 0)) {
+    if (L->exec) cudaGraphExecDestroy(L->exec);
+    if (L->graph) cudaGraphDestroy(L->graph);
+    L->exec = nullptr;
+    L->graph = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) return e;
+    L->graph = g;
+    cudaMemsetParams mp{};
+    mp.dst = ctl;
+    mp.value = 0;
+    mp.elementSize = 4;
+    mp.width = 2;
+    mp.height = 1;
+    cudaGraphNode_t mnode;
+    if ((e = cudaGraphAddMemsetNode(&mnode, g, nullptr, 0, &mp)) != cudaSuccess) return e;
+    cudaGraphConditionalHandle h;
+    if ((e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
+      return e;
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    if ((e = cudaGraphAddNode(&wnode, g, &mnode, nullptr, 1, &cp)) != cudaSuccess) return e;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaKernelNodeParams kp{};
+    kp.func = kern;
+    kp.gridDim = dim3(grid);
+    kp.blockDim = dim3(threads);
+    kp.sharedMemBytes = (unsigned)smem;
+    kp.kernelParams = kargs;
+    cudaGraphNode_t knode;
+    if ((e = cudaGraphAddKernelNode(&knode, body, nullptr, 0, &kp)) != cudaSuccess) return e;
+    TileQueue qq = q;
+    int* c = ctl;
+    unsigned capv = cap;
+    unsigned long long* pp = passes;
+    unsigned long long* ov = overflow;
+    void* cargs[] = {&qq, &c, &capv, &pp, &ov, &h};
+    cudaKernelNodeParams cpk{};
+    cpk.func = reinterpret_cast<void*>(k_pass_ctl);
+    cpk.gridDim = dim3(1);
+    cpk.blockDim = dim3(1);
+    cpk.kernelParams = cargs;
+    cudaGraphNode_t cnode;
+    if ((e = cudaGraphAddKernelNode(&cnode, body, &knode, 1, &cpk)) != cudaSuccess) return e;
+    cudaGraphExec_t x = nullptr;
+    if ((e = cudaGraphInstantiate(&x, g, 0)) != cudaSuccess) return e;
+    L->exec = x;
+    L->key = key;
+  }
+  return cudaGraphLaunch(L->exec, s);
+}
+
+void key_common(PassLoopKey& k, int& i, const TileQueue& q, const Geo& g, const InstDesc* inst,
+                const unsigned long long* counters, const unsigned long long* fault,
+                const int* ctl, unsigned cap, int K, int TB, int grid) {
+  auto put = [&](long long v) { k.v[i++] = v; };
+  put((long long)(uintptr_t)q.flag[0]); put((long long)(uintptr_t)q.flag[1]);
+  put((long long)(uintptr_t)q.list[0]); put((long long)(uintptr_t)q.list[1]);
+  put((long long)(uintptr_t)q.ctr); put((long long)(uintptr_t)inst);
+  put((long long)(uintptr_t)counters); put((long long)(uintptr_t)fault);
+  put((long long)(uintptr_t)ctl); put(cap); put(K); put(TB); put(grid);
+  put(g.Cp); put(g.Bp); put(g.NP); put(g.ntb); put(g.ntc);
 }
 
 }  // namespace
@@ -184,6 +314,82 @@ cudaError_t launch_pool_pr2d(const PoolPR<int>& p, int K, int regs, unsigned lon
                       : launch_kt<KK, BB, 40>(maps, p, fault, tiles, s);
   LF_PR2D(4, 8) LF_PR2D(4, 16) LF_PR2D(4, 32) LF_PR2D(8, 8) LF_PR2D(8, 16) LF_PR2D(8, 32)
 #undef LF_PR2D
+  return cudaErrorInvalidValue;
+}
+
+template <int K, int TB, int REGS>
+cudaError_t loop_kt(PassLoop* L, const PR2dMaps& maps, const PoolPR<int>& p,
+                    unsigned long long* fault, int tiles, int* ctl, unsigned cap,
+                    unsigned long long* passes, cudaStream_t s) {
+  using Ly = PR2dLayout<K, TB>;
+  int grid = 0;
+  void* kern = kt_setup<K, TB, REGS>(grid);
+  grid = std::max(1, std::min(grid, tiles));
+  PassLoopKey key{};
+  int i = 0;
+  key.v[i++] = 1;  // push/relabel
+  key_common(key, i, p.q, p.inst0.g, p.inst, p.counters, fault, ctl, cap, K, TB, grid);
+  key.v[i++] = REGS;
+  key.v[i++] = p.sweeps;
+  key.v[i++] = (long long)(uintptr_t)p.res;
+  key.v[i++] = (long long)(uintptr_t)p.exc;
+  key.v[i++] = (long long)(uintptr_t)p.h;
+  const int* cp = ctl;
+  void* kargs[] = {const_cast<PR2dMaps*>(&maps), const_cast<PoolPR<int>*>(&p), &fault, &cp};
+  return run_loop(L, key, kern, grid, Ly::NT, Ly::smem_bytes, kargs, p.q, ctl, cap, passes,
+                  nullptr, s);
+}
+
+template <int K, int TB>
+cudaError_t bfs_loop_kt(PassLoop* L, const BFS2dMaps& maps, const PoolBFS& p,
+                        unsigned long long* fault, int tiles, int* ctl, unsigned cap,
+                        unsigned long long* passes, unsigned long long* overflow,
+                        cudaStream_t s) {
+  using Ly = BFS2dLayout<TB>;
+  int grid = 0;
+  void* kern = bfs_kt_setup<K, TB>(grid);
+  grid = std::max(1, std::min(grid, tiles));
+  PassLoopKey key{};
+  int i = 0;
+  key.v[i++] = 2;  // BFS
+  key_common(key, i, p.q, p.inst0.g, p.inst, p.counters, fault, ctl, cap, K, TB, grid);
+  key.v[i++] = p.max_local;
+  key.v[i++] = (long long)(uintptr_t)p.h;
+  key.v[i++] = (long long)(uintptr_t)p.mask;
+  key.v[i++] = (long long)(uintptr_t)p.any_changed;
+  key.v[i++] = (long long)(uintptr_t)overflow;
+  const int* cp = ctl;
+  void* kargs[] = {const_cast<BFS2dMaps*>(&maps), const_cast<PoolBFS*>(&p), &fault, &cp};
+  return run_loop(L, key, kern, grid, Ly::NT, Ly::smem_bytes, kargs, p.q, ctl, cap, passes,
+                  overflow, s);
+}
+
+cudaError_t loop_pool_pr2d(PassLoop* L, const PoolPR<int>& p, int K, int regs,
+                           unsigned long long* fault, int tiles, int* ctl, unsigned cap,
+                           unsigned long long* passes, cudaStream_t s) {
+  PR2dMaps maps;
+  if (!maps_for(p, K, p.inst0.g.TB, maps)) return cudaErrorInvalidValue;
+  const int TB = p.inst0.g.TB;
+#define LF_PR2D(KK, BB)                                                                      \
+  if (K == KK && TB == BB)                                                                     \
+    return regs == 32 ? loop_kt<KK, BB, 32>(L, maps, p, fault, tiles, ctl, cap, passes, s)     \
+                      : loop_kt<KK, BB, 40>(L, maps, p, fault, tiles, ctl, cap, passes, s);
+  LF_PR2D(4, 8) LF_PR2D(4, 16) LF_PR2D(4, 32) LF_PR2D(8, 8) LF_PR2D(8, 16) LF_PR2D(8, 32)
+#undef LF_PR2D
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t loop_pool_bfs2d(PassLoop* L, const PoolBFS& p, int K, unsigned long long* fault,
+                            int tiles, int* ctl, unsigned cap, unsigned long long* passes,
+                            unsigned long long* overflow, cudaStream_t s) {
+  BFS2dMaps maps;
+  const int TB = p.inst0.g.TB;
+  if (!bfs_maps_for(p, TB, maps)) return cudaErrorInvalidValue;
+#define LF_BFS2D(KK, BB)                                                                      \
+  if (K == KK && TB == BB)                                                                      \
+    return bfs_loop_kt<KK, BB>(L, maps, p, fault, tiles, ctl, cap, passes, overflow, s);
+  LF_BFS2D(4, 8) LF_BFS2D(4, 16) LF_BFS2D(4, 32) LF_BFS2D(8, 8) LF_BFS2D(8, 16) LF_BFS2D(8, 32)
+#undef LF_BFS2D
   return cudaErrorInvalidValue;
 }
 

@@ -151,7 +151,7 @@ __device__ __forceinline__ void pr2d_issue(const PR2dMaps& maps, const Geo& g, i
 // push into s_exc at once, and a later read would miss the flow they sent,
 // which the delta write-back of the excess needs).
 template <int K, int TB>
-__device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const Geo& g, int hmax,
+__device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const Geo& g, int hmax, int cur,
                                           unsigned char* stage, int tile, const int e0,
                                           int my_h) {
   using Ly = PR2dLayout<K, TB>;
@@ -166,7 +166,7 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const Geo& g, in
   const int b0 = tb * TB, c0 = tc * 32;
   const long long gi = (long long)(b0 + ib) * g.Cp + (c0 + ic);
   const int hidx = (ib + 1) * HW + (ic + 4);
-  const int nxt = p.cur ^ 1;
+  const int nxt = cur ^ 1;
   // directions that leave the tile
   unsigned outm = 0;
 #pragma unroll
@@ -251,10 +251,14 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const Geo& g, in
 // `fault` (global) records a copy that did not land in time.  REGS caps the
 // registers per thread: 40 keeps three 512-thread tiles on an SM without
 // spills, 32 fits four (with a few spilled values for 8 directions).
+// ctl: null for a launch of its own (list, height cap and finished flag from
+// the parameters); else the pass runs inside a device-side loop of passes
+// (a CUDA graph) and reads the list to consume from ctl[0] and the height
+// cap and finished flag from the lattice's descriptor in device memory.
 template <int K, int TB, int REGS>
 __global__ void __maxnreg__(REGS)
     k_pool_pr2d(const __grid_constant__ PR2dMaps maps, PoolPR<int> p,
-                unsigned long long* fault) {
+                unsigned long long* fault, const int* ctl) {
   using Ly = PR2dLayout<K, TB>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
@@ -262,24 +266,25 @@ __global__ void __maxnreg__(REGS)
   const unsigned bar0 = smem_addr(smem + 2 * Ly::stage_bytes);  // two mbarriers, 8 bytes apart
   const unsigned stage0 = smem_addr(smem);
   const Geo& g = p.inst0.g;
-  const int hmax = p.inst0.hmax;
-  const unsigned n = queued_count(p.q, p.cur);
-  const int* list = p.q.list[p.cur];
+  const int cur = ctl ? *ctl : p.cur;
+  const unsigned n = queued_count(p.q, cur);
+  const int* list = p.q.list[cur];
   if (blockIdx.x >= n) return;
+  const int hmax = ctl ? p.inst[0].hmax : p.inst0.hmax;
   if (threadIdx.x == 0) {
     mbar_init(bar0, 1);
     mbar_init(bar0 + 8, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  const bool done = p.inst0.done != 0;
+  const bool done = (ctl ? p.inst[0].done : p.inst0.done) != 0;
   if (threadIdx.x == 0 && !done) pr2d_issue<K, TB>(maps, g, list[blockIdx.x], stage0, bar0);
   unsigned phases = 0;  // bit b: parity of the next phase of buffer b
   unsigned buf = 0;
   for (unsigned i = blockIdx.x; i < n; i += gridDim.x, buf ^= 1) {
     const int gt = list[i];
     if (threadIdx.x == 0) {
-      p.q.flag[p.cur][gt] = 0;
+      p.q.flag[cur][gt] = 0;
       atomicAdd(&p.counters[0], 1ull);
     }
     if (done) continue;
@@ -306,7 +311,7 @@ __global__ void __maxnreg__(REGS)
       if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
       return;
     }
-    pr2d_tile<K, TB>(p, g, hmax, st, gt, e0, h0);
+    pr2d_tile<K, TB>(p, g, hmax, cur, st, gt, e0, h0);
   }
 }
 

@@ -29,6 +29,8 @@ struct Tuning {
                                  // with 32 registers
   int bfs_kernel = 0;            // BFS pass of a single 2-d lattice: 0 = TMA-staged,
                                  // 1 = generic tile kernel
+  int host_loops = 0;            // TMA-staged passes: 0 = device-side pass loops (CUDA
+                                 // graphs), 1 = one launch per pass from the host
 };
 
 struct SolveStats {
@@ -87,6 +89,21 @@ cudaError_t launch_pool_pr2d(const PoolPR<int>& p, int K, int regs, unsigned lon
                              int tiles, cudaStream_t s);
 cudaError_t launch_pool_bfs2d(const PoolBFS& p, int K, unsigned long long* fault, int tiles,
                               cudaStream_t s);
+
+// Device-side loops of those passes (one CUDA graph launch runs passes until
+// the next tile list is empty or `cap` passes ran; ctl: two device words the
+// loop keeps its list index and pass count in; passes: incremented per pass;
+// overflow: set when the cap ends a loop that still had tiles queued).  A
+// PassLoop caches the instantiated graph for the arrays it was built for.
+struct PassLoop;
+PassLoop* pass_loop_new();
+void pass_loop_free(PassLoop* L);
+cudaError_t loop_pool_pr2d(PassLoop* L, const PoolPR<int>& p, int K, int regs,
+                           unsigned long long* fault, int tiles, int* ctl, unsigned cap,
+                           unsigned long long* passes, cudaStream_t s);
+cudaError_t loop_pool_bfs2d(PassLoop* L, const PoolBFS& p, int K, unsigned long long* fault,
+                            int tiles, int* ctl, unsigned cap, unsigned long long* passes,
+                            unsigned long long* overflow, cudaStream_t s);
 
 cudaError_t launch_pool_bfs(const PoolBFS& p, int KA, int KB, bool single, int grid, int threads,
                             size_t smem, cudaStream_t s);
@@ -157,7 +174,12 @@ class PoolRunner {
   long long* d_sum = nullptr;
   int* d_flag = nullptr;
   unsigned long long* d_counters = nullptr;  // [0] pr tiles, [1] bfs tiles, [2] tail moved,
-                                             // [3] active total, [4] staging fault
+                                             // [3] active total, [4] staging fault, [5] bfs
+                                             // passes and [6] pr passes of device-side loops,
+                                             // [7] a device-side BFS loop hit its cap
+  int* d_ctl = nullptr;                      // control words of the device-side loops
+  PassLoop* loop_pr = nullptr;
+  PassLoop* loop_bfs = nullptr;
   void* h_pin = nullptr;
   int threads = 1, hv_max = 0;
   int ka = 0, kb = 0;  // kernel sizes present in the pool
