@@ -30,6 +30,11 @@ namespace {
 
 inline int nblk(long long n, int t) { return int((n + t - 1) / t); }
 
+// tuning value pr_kernel -> variant of the TMA-staged push/relabel pass
+inline int pr2d_variant(int pr_kernel) {
+  return pr_kernel == 2 ? 1 : 0;
+}
+
 // lattice of pool node i (node_base ascending, n entries + sentinel)
 __device__ __forceinline__ int inst_of(const long long* nbase, int n, long long i) {
   int lo = 0, hi = n;  // nbase[lo] <= i < nbase[hi]
@@ -84,6 +89,54 @@ __global__ void k_pool_mask(const InstDesc* insts, const long long* nbase, int n
     if (r[(long long)k * I.plane + li] > 0) m |= 1ull << k;
   if (kmask) m &= kmask[i];
   mask[i] = m;
+}
+
+// The set-up of a global relabel for a pool of one lattice in one pass:
+// initial heights (0 at deficits of the lattice's sections, else kHInf),
+// residual masks, and every tile queued in list 0.  Four nodes (32-bit) or
+// two (64-bit) per thread, one 16-byte load per residual plane.
+template <typename T>
+__global__ void k_relabel_init1(const InstDesc* insts, long long NP, const T* res, const T* exc,
+                                const uint64_t* kmask, int* h, uint64_t* mask, TileQueue q,
+                                int tiles) {
+  constexpr int VW = 16 / sizeof(T);
+  using V = typename std::conditional<sizeof(T) == 4, int4, longlong2>::type;
+  const InstDesc& I = insts[0];
+  if (I.done || !I.active) return;
+  const int K = I.st.K;
+  const long long plane = I.plane;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v * VW < NP; v += stride) {
+    const long long i0 = v * VW;
+    uint64_t m[VW];
+#pragma unroll
+    for (int j = 0; j < VW; ++j) m[j] = 0;
+    for (int k = 0; k < K; ++k) {
+      const V r = *reinterpret_cast<const V*>(res + (long long)k * plane + i0);
+      const T* rv = reinterpret_cast<const T*>(&r);
+#pragma unroll
+      for (int j = 0; j < VW; ++j)
+        if (rv[j] > 0) m[j] |= 1ull << k;
+    }
+    const V e = *reinterpret_cast<const V*>(exc + i0);
+    const T* ev = reinterpret_cast<const T*>(&e);
+#pragma unroll
+    for (int j = 0; j < VW; ++j) {
+      bool part = true;
+      if (kmask) {
+        const uint64_t km = kmask[i0 + j];
+        m[j] &= km;
+        part = (km >> 63) != 0;
+      }
+      mask[i0 + j] = m[j];
+      h[i0 + j] = (part && ev[j] < 0) ? 0 : kHInf;
+    }
+  }
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tiles; t += stride) {
+    q.flag[0][t] = 1;
+    q.list[0][t] = (int)t;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 4) q.ctr[threadIdx.x] = threadIdx.x == q_count_idx(0) ? tiles : 0;
 }
 
 // every tile of every unfinished lattice into list 0
@@ -462,13 +515,19 @@ template <typename T>
 void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* mask,
                                 const uint64_t* kmask, SolveStats& stats) {
   const int B = 256;
-  k_pool_init_heights<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, exc, kmask, h);
-  count_launch();
-  k_pool_mask<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, res, kmask, mask);
-  count_launch();
-  check(cudaMemsetAsync(q.ctr, 0, 4 * sizeof(unsigned), stream), "memset");
-  k_pool_queue_all<<<nblk(tiles, B), B, 0, stream>>>(d_inst, d_tile_inst, tiles, q);
-  count_launch();
+  if (n == 1) {  // NP is a multiple of 32 and every plane 16-byte aligned
+    k_relabel_init1<T><<<std::min(nblk(NP / (16 / sizeof(T)), B), 152 * 8), B, 0, stream>>>(
+        d_inst, NP, res, exc, kmask, h, mask, q, tiles);
+    count_launch();
+  } else {
+    k_pool_init_heights<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, exc, kmask, h);
+    count_launch();
+    k_pool_mask<T><<<nblk(NP, B), B, 0, stream>>>(d_inst, d_nbase, n, NP, res, kmask, mask);
+    count_launch();
+    check(cudaMemsetAsync(q.ctr, 0, 4 * sizeof(unsigned), stream), "memset");
+    k_pool_queue_all<<<nblk(tiles, B), B, 0, stream>>>(d_inst, d_tile_inst, tiles, q);
+    count_launch();
+  }
   check(cudaGetLastError(), "bfs setup");
   const size_t smem = sizeof(PoolSmemHead) + size_t(hv_max) * sizeof(int);
   const int grid = std::max(tiles, 1);
@@ -616,7 +675,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
         // M passes (fewer when the queue runs dry) in one device-side loop
         if (!loop_pr) loop_pr = pass_loop_new();
         mark(0, false);
-        check(loop_pool_pr2d(loop_pr, p, k2d, tune.pr_kernel == 2 ? 32 : 40, d_counters + 4,
+        check(loop_pool_pr2d(loop_pr, p, k2d, pr2d_variant(tune.pr_kernel), d_counters + 4,
                              std::max(tiles, 1), d_ctl, (unsigned)M, d_counters + 6, stream),
               "push-relabel loop (TMA)");
         mark(0, true);
@@ -635,7 +694,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
         if (tune.pr_kernel != 1) k2d = pr2d_kernel_size(p, n == 1);
       if (k2d) {
         if constexpr (std::is_same<T, int>::value)
-          check(launch_pool_pr2d(p, k2d, tune.pr_kernel == 2 ? 32 : 40, d_counters + 4,
+          check(launch_pool_pr2d(p, k2d, pr2d_variant(tune.pr_kernel), d_counters + 4,
                                  std::max(tiles, 1), stream),
                 "push-relabel pass (TMA)");
       } else {

@@ -303,15 +303,16 @@ int pr2d_kernel_size(const PoolPR<int>& p, bool single) {
   return p.kmask ? 0 : lattice2d_kernel_size(p.inst0, single);
 }
 
-cudaError_t launch_pool_pr2d(const PoolPR<int>& p, int K, int regs, unsigned long long* fault,
+cudaError_t launch_pool_pr2d(const PoolPR<int>& p, int K, int variant, unsigned long long* fault,
                              int tiles, cudaStream_t s) {
   PR2dMaps maps;
   if (!maps_for(p, K, p.inst0.g.TB, maps)) return cudaErrorInvalidValue;
   const int TB = p.inst0.g.TB;
-#define LF_PR2D(KK, BB)                                                              \
-  if (K == KK && TB == BB)                                                             \
-    return regs == 32 ? launch_kt<KK, BB, 32>(maps, p, fault, tiles, s)                \
-                      : launch_kt<KK, BB, 40>(maps, p, fault, tiles, s);
+#define LF_PR2D(KK, BB)                                                                \
+  if (K == KK && TB == BB) {                                                             \
+    if (variant == 1) return launch_kt<KK, BB, 32>(maps, p, fault, tiles, s);            \
+    return launch_kt<KK, BB, 40>(maps, p, fault, tiles, s);                              \
+  }
   LF_PR2D(4, 8) LF_PR2D(4, 16) LF_PR2D(4, 32) LF_PR2D(8, 8) LF_PR2D(8, 16) LF_PR2D(8, 32)
 #undef LF_PR2D
   return cudaErrorInvalidValue;
@@ -364,16 +365,17 @@ cudaError_t bfs_loop_kt(PassLoop* L, const BFS2dMaps& maps, const PoolBFS& p,
                   overflow, s);
 }
 
-cudaError_t loop_pool_pr2d(PassLoop* L, const PoolPR<int>& p, int K, int regs,
+cudaError_t loop_pool_pr2d(PassLoop* L, const PoolPR<int>& p, int K, int variant,
                            unsigned long long* fault, int tiles, int* ctl, unsigned cap,
                            unsigned long long* passes, cudaStream_t s) {
   PR2dMaps maps;
   if (!maps_for(p, K, p.inst0.g.TB, maps)) return cudaErrorInvalidValue;
   const int TB = p.inst0.g.TB;
 #define LF_PR2D(KK, BB)                                                                      \
-  if (K == KK && TB == BB)                                                                     \
-    return regs == 32 ? loop_kt<KK, BB, 32>(L, maps, p, fault, tiles, ctl, cap, passes, s)     \
-                      : loop_kt<KK, BB, 40>(L, maps, p, fault, tiles, ctl, cap, passes, s);
+  if (K == KK && TB == BB) {                                                                   \
+    if (variant == 1) return loop_kt<KK, BB, 32>(L, maps, p, fault, tiles, ctl, cap, passes, s); \
+    return loop_kt<KK, BB, 40>(L, maps, p, fault, tiles, ctl, cap, passes, s);                  \
+  }
   LF_PR2D(4, 8) LF_PR2D(4, 16) LF_PR2D(4, 32) LF_PR2D(8, 8) LF_PR2D(8, 16) LF_PR2D(8, 32)
 #undef LF_PR2D
   return cudaErrorInvalidValue;

@@ -85,7 +85,8 @@ cudaError_t launch_pool_pr(const PoolPR<T>& p, int KA, int KB, int threads, size
 // takes no section mask).
 int lattice2d_kernel_size(const InstDesc& I, bool single);
 int pr2d_kernel_size(const PoolPR<int>& p, bool single);
-cudaError_t launch_pool_pr2d(const PoolPR<int>& p, int K, int regs, unsigned long long* fault,
+// variant: 0 = at most 40 registers per thread, 1 = at most 32
+cudaError_t launch_pool_pr2d(const PoolPR<int>& p, int K, int variant, unsigned long long* fault,
                              int tiles, cudaStream_t s);
 cudaError_t launch_pool_bfs2d(const PoolBFS& p, int K, unsigned long long* fault, int tiles,
                               cudaStream_t s);
@@ -98,7 +99,7 @@ cudaError_t launch_pool_bfs2d(const PoolBFS& p, int K, unsigned long long* fault
 struct PassLoop;
 PassLoop* pass_loop_new();
 void pass_loop_free(PassLoop* L);
-cudaError_t loop_pool_pr2d(PassLoop* L, const PoolPR<int>& p, int K, int regs,
+cudaError_t loop_pool_pr2d(PassLoop* L, const PoolPR<int>& p, int K, int variant,
                            unsigned long long* fault, int tiles, int* ctl, unsigned cap,
                            unsigned long long* passes, cudaStream_t s);
 cudaError_t loop_pool_bfs2d(PassLoop* L, const PoolBFS& p, int K, unsigned long long* fault,
