@@ -16,9 +16,9 @@ import math
 import os
 
 DEFAULT_GRID = {
-    "tile_rows": (16, 32),
-    "local_sweeps": (2, 4, 8),
-    "launches_per_relabel": (2, 4, 8),
+    "tile_rows": (8, 16, 32),
+    "local_sweeps": (1, 2, 4),
+    "launches_per_relabel": (4, 8, 16),
 }
 
 _memory = {}

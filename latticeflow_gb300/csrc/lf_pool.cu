@@ -383,6 +383,8 @@ void PoolRunner::release() {
   if (loop_pr) pass_loop_free(loop_pr);
   if (loop_bfs) pass_loop_free(loop_bfs);
   loop_pr = loop_bfs = nullptr;
+  if (pool_maps) pool_maps_free(pool_maps);
+  pool_maps = nullptr;
   if (h_pin) { cudaFreeHost(h_pin); h_pin = nullptr; }
   free_tail();
 }
@@ -547,6 +549,24 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
     count_launch();
     return;
   }
+  // a pool of 2-d lattices: the TMA-staged pass with each lattice's maps
+  const int tb_pool = (!k2d && n > 1 && tune.bfs_kernel != 1) ? pool2d_tile_rows(host) : 0;
+  const void* maps = nullptr;
+  if (tb_pool) {
+    if (!pool_maps) pool_maps = pool_maps_new();
+    maps = pool_maps_bfs(pool_maps, host, h, mask, stream);
+  }
+  if (maps && tune.host_loops != 1) {
+    if (!loop_bfs) loop_bfs = pass_loop_new();
+    PoolBFS p{host[0], d_inst, d_tile_inst, h, mask, q, 0, 64, d_flag, d_counters};
+    mark(1, false);
+    check(pool_bfs2d(loop_bfs, maps, p, tb_pool, d_counters + 4, grid, d_ctl, (unsigned)cap,
+                     d_counters + 5, d_counters + 7, stream),
+          "bfs loop (TMA, pool)");
+    mark(1, true);
+    count_launch();
+    return;
+  }
   int cur = 0;
   for (long long pass = 0;;) {
     if (pass > cap) throw LfError{4, "global relabel did not converge"};
@@ -556,6 +576,10 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
       PoolBFS p{host[0], d_inst, d_tile_inst, h, mask, q, cur, 64, d_flag, d_counters};
       mark(1, false);
       if (k2d) check(launch_pool_bfs2d(p, k2d, d_counters + 4, grid, stream), "bfs pass (TMA)");
+      else if (maps)
+        check(pool_bfs2d(nullptr, maps, p, tb_pool, d_counters + 4, grid, nullptr, 0, nullptr,
+                         nullptr, stream),
+              "bfs pass (TMA, pool)");
       else check(launch_pool_bfs(p, ka, kb, n == 1, grid, threads, smem, stream), "bfs pass");
       check(cudaGetLastError(), "bfs pass");
       mark(1, true);
@@ -668,9 +692,27 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
         continue;
       }
     }
+    const void* pmaps = nullptr;  // pool of 2-d lattices: the TMA-staged pass
+    int tb_pool = 0;
     if constexpr (std::is_same<T, int>::value) {
       PoolPR<int> p{host[0], d_inst, d_tile_inst, res, exc, h, kmask, q, 0, R, d_counters};
       const int k2d = tune.pr_kernel != 1 ? pr2d_kernel_size(p, n == 1) : 0;
+      tb_pool = (!k2d && n > 1 && !kmask && tune.pr_kernel != 1) ? pool2d_tile_rows(host) : 0;
+      if (tb_pool) {
+        if (!pool_maps) pool_maps = pool_maps_new();
+        pmaps = pool_maps_pr(pool_maps, host, res, exc, h, stream);
+      }
+      if (pmaps && tune.host_loops != 1) {
+        if (!loop_pr) loop_pr = pass_loop_new();
+        mark(0, false);
+        check(pool_pr2d(loop_pr, pmaps, p, tb_pool, pr2d_variant(tune.pr_kernel), d_counters + 4,
+                        std::max(tiles, 1), d_ctl, (unsigned)M, d_counters + 6, stream),
+              "push-relabel loop (TMA, pool)");
+        mark(0, true);
+        count_launch();
+        drain_queue();
+        continue;
+      }
       if (k2d && tune.host_loops != 1) {
         // M passes (fewer when the queue runs dry) in one device-side loop
         if (!loop_pr) loop_pr = pass_loop_new();
@@ -697,6 +739,11 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
           check(launch_pool_pr2d(p, k2d, pr2d_variant(tune.pr_kernel), d_counters + 4,
                                  std::max(tiles, 1), stream),
                 "push-relabel pass (TMA)");
+      } else if (pmaps) {
+        if constexpr (std::is_same<T, int>::value)
+          check(pool_pr2d(nullptr, pmaps, p, tb_pool, pr2d_variant(tune.pr_kernel), d_counters + 4,
+                          std::max(tiles, 1), nullptr, 0, nullptr, stream),
+                "push-relabel pass (TMA, pool)");
       } else {
         check(launch_pool_pr<T>(p, KA, KB, NTmax, smem, n == 1, std::max(tiles, 1), stream),
               "push-relabel pass");

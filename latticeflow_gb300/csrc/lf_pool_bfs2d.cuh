@@ -64,17 +64,18 @@ __device__ __forceinline__ unsigned bfs2d_edge_bits(int ib, int ic) {
   return b;
 }
 
-template <int K, int TB>
-__device__ __forceinline__ void bfs2d_tile(const PoolBFS& p, const Geo& g, int cur,
+// LAT as for pr2d_tile.
+template <int K, int TB, class LAT>
+__device__ __forceinline__ void bfs2d_tile(const PoolBFS& p, const LAT& L, int cur,
                                            unsigned char* stage, unsigned* s_flags, int tile,
                                            int my_h, const uint64_t m) {
-  using Ly = BFS2dLayout<TB>;
   constexpr int HW = kPr2dHaloW;
   int* s_h = reinterpret_cast<int*>(stage);
   const int t = threadIdx.x;
   const int ic = t & 31, ib = t >> 5;
-  const int tc = tile % g.ntc, tb = tile / g.ntc;
-  const long long gi = (long long)(tb * TB + ib) * g.Cp + (tc * 32 + ic);
+  const int tc = tile % lat_ntc(L), tb = tile / lat_ntc(L);
+  const long long gi = (long long)(tb * TB + ib) * lat_Cp(L) + (tc * 32 + ic) + lat_node_base(L);
+  const int tile_g = lat_tile_base(L) + tile;
   const int hidx = (ib + 1) * HW + (ic + 4);
   const int nxt = cur ^ 1;
   // the row directions of both stencils: (0, 1) is entry 0, (0, -1) entry K/2
@@ -114,11 +115,12 @@ __device__ __forceinline__ void bfs2d_tile(const PoolBFS& p, const Geo& g, int c
     const int dtb = (t == 0 || t == 4 || t == 5) ? -1 : (t == 1 || t == 6 || t == 7) ? 1 : 0;
     const int dtc = (t == 2 || t == 4 || t == 6) ? -1 : (t == 3 || t == 5 || t == 7) ? 1 : 0;
     const int a = tb + dtb, c = tc + dtc;
-    if (a >= 0 && a < g.ntb && c >= 0 && c < g.ntc) enqueue_tile(p.q, nxt, a * g.ntc + c);
+    if (a >= 0 && a < lat_ntb(L) && c >= 0 && c < lat_ntc(L))
+      enqueue_tile(p.q, nxt, lat_tile_base(L) + a * lat_ntc(L) + c);
   }
   if (t == 0) {
     if (f) *p.any_changed = 1;
-    if (!converged) { enqueue_tile(p.q, nxt, tile); *p.any_changed = 1; }
+    if (!converged) { enqueue_tile(p.q, nxt, tile_g); *p.any_changed = 1; }
   }
 }
 
@@ -178,6 +180,87 @@ __global__ void __launch_bounds__(TB * 32, 2048 / (TB * 32))
       return;
     }
     bfs2d_tile<K, TB>(p, g, cur, st, s_flags + buf, gt, h0, m);
+  }
+}
+
+// A lattice's two tensor maps (heights, masks) in the pool's map array.
+template <int TB>
+__device__ __forceinline__ void bfs2d_pool_issue(const PoolBFS& p, const CUtensorMap* maps, int gt,
+                                                 unsigned stage, unsigned bar) {
+  using Ly = BFS2dLayout<TB>;
+  const int ii = p.tile_inst[gt];
+  const InstDesc& I = p.inst[ii];
+  const int tile = gt - I.tile_base;
+  const int tc = tile % I.g.ntc, tb = tile / I.g.ntc;
+  const int b0 = tb * TB, c0 = tc * 32;
+  mbar_expect_tx(bar, Ly::tx_bytes);
+  tma_load_2d(stage, &maps[2 * ii], c0 - 4, b0 - 1, bar);
+  tma_load_2d(stage + Ly::mask_off, &maps[2 * ii + 1], c0, b0, bar);
+}
+
+// Many 2-d lattices (Full2d_4 / Full2d_8, one tile height) in one pool, any
+// capacity type: the same pass as k_pool_bfs2d with each tile's own
+// lattice, stencil and tensor maps.
+template <int TB>
+__global__ void __launch_bounds__(TB * 32, 2048 / (TB * 32))
+    k_pool_bfs2d_pool(const CUtensorMap* maps, PoolBFS p, unsigned long long* fault,
+                      const int* ctl) {
+  using Ly = BFS2dLayout<TB>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<unsigned long long>(smem_raw) + 127) & ~127ull);
+  const unsigned bar0 = smem_addr(smem + 2 * Ly::stage_bytes);
+  unsigned* s_flags = reinterpret_cast<unsigned*>(smem + 2 * Ly::stage_bytes + 16);
+  const unsigned stage0 = smem_addr(smem);
+  const int cur = ctl ? *ctl : p.cur;
+  const unsigned n = queued_count(p.q, cur);
+  const int* list = p.q.list[cur];
+  if (blockIdx.x >= n) return;
+  if (threadIdx.x == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar0 + 8, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) bfs2d_pool_issue<TB>(p, maps, list[blockIdx.x], stage0, bar0);
+  unsigned phases = 0;
+  unsigned buf = 0;
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x, buf ^= 1) {
+    const int gt = list[i];
+    if (threadIdx.x == 0) {
+      p.q.flag[cur][gt] = 0;
+      atomicAdd(&p.counters[1], 1ull);
+      s_flags[buf] = 0;
+    }
+    const unsigned nx = i + gridDim.x;
+    if (threadIdx.x == 0 && nx < n)
+      bfs2d_pool_issue<TB>(p, maps, list[nx], stage0 + (buf ^ 1) * Ly::stage_bytes,
+                           bar0 + (buf ^ 1) * 8);
+    const unsigned bar = bar0 + buf * 8;
+    const unsigned par = (phases >> buf) & 1u;
+    const bool ok = mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+    phases ^= 1u << buf;
+    unsigned char* st = smem + buf * Ly::stage_bytes;
+    const int h0 = reinterpret_cast<const int*>(st)[((threadIdx.x >> 5) + 1) * kPr2dHaloW +
+                                                     (threadIdx.x & 31) + 4];
+    const uint64_t m = reinterpret_cast<const uint64_t*>(st + Ly::mask_off)[threadIdx.x];
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicExch(fault, 1ull);
+      mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+      if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
+      return;
+    }
+    const InstDesc& I = p.inst[p.tile_inst[gt]];
+    if (I.done) {  // the whole block reads the same flag
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      continue;
+    }
+    const Lat2d L = lat2d_of(I);
+    const int tile = gt - L.tile_base;
+    if (I.st.K == 8)
+      bfs2d_tile<8, TB>(p, L, cur, st, s_flags + buf, tile, h0, m);
+    else
+      bfs2d_tile<4, TB>(p, L, cur, st, s_flags + buf, tile, h0, m);
   }
 }
 

@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "lf_pool_bfs2d.cuh"
 #include "lf_pool_pr2d.cuh"
@@ -192,7 +193,137 @@ __global__ void k_pass_ctl(TileQueue q, int* ctl, unsigned cap, unsigned long lo
   cudaGraphSetConditional(h, (n > 0 && run < cap) ? 1u : 0u);
 }
 
+template <int TB, int REGS>
+void* kt_pool_setup(int& grid) {
+  using Ly = PR2dPoolLayout<TB>;
+  auto kern = k_pool_pr2d_pool<TB, REGS>;
+  static std::mutex mu;
+  static int cap = 0;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!cap) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Ly::smem_bytes);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cap = occupancy_grid(kern, Ly::NT, Ly::smem_bytes);
+  }
+  grid = cap;
+  return reinterpret_cast<void*>(kern);
+}
+
+template <int TB>
+void* bfs_kt_pool_setup(int& grid) {
+  using Ly = BFS2dLayout<TB>;
+  auto kern = k_pool_bfs2d_pool<TB>;
+  static std::mutex mu;
+  static int cap = 0;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!cap) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Ly::smem_bytes);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cap = occupancy_grid(kern, Ly::NT, Ly::smem_bytes);
+  }
+  grid = cap;
+  return reinterpret_cast<void*>(kern);
+}
+
 }  // namespace
+
+// Tensor maps of every lattice of a pool, in device memory: three per
+// lattice for the push/relabel pass (residual planes, excess, heights; int32
+// arrays) and two for the BFS pass (heights, masks).  Rebuilt when the
+// arrays move.
+struct PoolMaps {
+  void* d_pr = nullptr;
+  void* d_bfs = nullptr;
+  size_t pr_n = 0, bfs_n = 0;
+  const void* pr_key[3] = {nullptr, nullptr, nullptr};
+  const void* bfs_key[2] = {nullptr, nullptr};
+  ~PoolMaps() {
+    cudaFree(d_pr);
+    cudaFree(d_bfs);
+  }
+};
+
+PoolMaps* pool_maps_new() { return new PoolMaps(); }
+void pool_maps_free(PoolMaps* m) { delete m; }
+
+int pool2d_tile_rows(const std::vector<InstDesc>& insts) {
+  if (insts.size() < 2 || !encode_fn()) return 0;
+  const int TB = insts[0].g.TB;
+  if (TB != 8 && TB != 16 && TB != 32) return 0;
+  for (const InstDesc& I : insts) {
+    if (I.g.TB != TB || I.g.TA != 1 || I.g.A != 1 || I.g.Ap != 1 || I.g.TC != 32) return 0;
+    if (I.g.Cp % 32 || I.g.Bp % TB) return 0;
+    if (!stencil_is<4>(I.st) && !stencil_is<8>(I.st)) return 0;
+    // 16-byte aligned bases and plane strides for the tensor maps
+    if (I.node_base % 4 || I.res_base % 4 || I.plane % 4) return 0;
+  }
+  return TB;
+}
+
+const void* pool_maps_pr(PoolMaps* M, const std::vector<InstDesc>& insts, int* res, int* exc,
+                         int* h, cudaStream_t s) {
+  if (M->d_pr && M->pr_key[0] == res && M->pr_key[1] == exc && M->pr_key[2] == h &&
+      M->pr_n == insts.size())
+    return M->d_pr;
+  std::vector<CUtensorMap> maps(3 * insts.size());
+  for (size_t i = 0; i < insts.size(); ++i) {
+    const InstDesc& I = insts[i];
+    const Geo& g = I.g;
+    const int TB = g.TB;
+    const cuuint64_t d3[3] = {(cuuint64_t)g.Cp, (cuuint64_t)g.Bp, (cuuint64_t)I.st.K};
+    const cuuint64_t s3[2] = {(cuuint64_t)g.Cp * 4, (cuuint64_t)I.plane * 4};
+    const cuuint32_t b3[3] = {32, (cuuint32_t)TB, (cuuint32_t)I.st.K};
+    const cuuint64_t d2[2] = {(cuuint64_t)g.Cp, (cuuint64_t)g.Bp};
+    const cuuint64_t s2[1] = {(cuuint64_t)g.Cp * 4};
+    const cuuint32_t be[2] = {32, (cuuint32_t)TB};
+    const cuuint32_t bh[2] = {(cuuint32_t)kPr2dHaloW, (cuuint32_t)(TB + 2)};
+    if (!encode(&maps[3 * i], res + I.res_base, 3, d3, s3, b3) ||
+        !encode(&maps[3 * i + 1], exc + I.node_base, 2, d2, s2, be) ||
+        !encode(&maps[3 * i + 2], h + I.node_base, 2, d2, s2, bh))
+      return nullptr;
+  }
+  cudaFree(M->d_pr);
+  M->d_pr = nullptr;
+  const size_t bytes = maps.size() * sizeof(CUtensorMap);
+  if (cudaMalloc(&M->d_pr, bytes) != cudaSuccess) return nullptr;
+  if (cudaMemcpyAsync(M->d_pr, maps.data(), bytes, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return nullptr;
+  M->pr_key[0] = res; M->pr_key[1] = exc; M->pr_key[2] = h;
+  M->pr_n = insts.size();
+  return M->d_pr;
+}
+
+const void* pool_maps_bfs(PoolMaps* M, const std::vector<InstDesc>& insts, int* h,
+                          const uint64_t* mask, cudaStream_t s) {
+  if (M->d_bfs && M->bfs_key[0] == h && M->bfs_key[1] == mask && M->bfs_n == insts.size())
+    return M->d_bfs;
+  std::vector<CUtensorMap> maps(2 * insts.size());
+  for (size_t i = 0; i < insts.size(); ++i) {
+    const InstDesc& I = insts[i];
+    const Geo& g = I.g;
+    const int TB = g.TB;
+    const cuuint64_t d2[2] = {(cuuint64_t)g.Cp, (cuuint64_t)g.Bp};
+    const cuuint64_t s4[1] = {(cuuint64_t)g.Cp * 4};
+    const cuuint64_t s8[1] = {(cuuint64_t)g.Cp * 8};
+    const cuuint32_t bh[2] = {(cuuint32_t)kPr2dHaloW, (cuuint32_t)(TB + 2)};
+    const cuuint32_t bm[2] = {32, (cuuint32_t)TB};
+    if (!encode(&maps[2 * i], h + I.node_base, 2, d2, s4, bh) ||
+        !encode(&maps[2 * i + 1], const_cast<uint64_t*>(mask) + I.node_base, 2, d2, s8, bm,
+                CU_TENSOR_MAP_DATA_TYPE_UINT64))
+      return nullptr;
+  }
+  cudaFree(M->d_bfs);
+  M->d_bfs = nullptr;
+  const size_t bytes = maps.size() * sizeof(CUtensorMap);
+  if (cudaMalloc(&M->d_bfs, bytes) != cudaSuccess) return nullptr;
+  if (cudaMemcpyAsync(M->d_bfs, maps.data(), bytes, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return nullptr;
+  M->bfs_key[0] = h; M->bfs_key[1] = mask;
+  M->bfs_n = insts.size();
+  return M->d_bfs;
+}
 
 // What a pass loop was built for: it is rebuilt when any of these changes.
 struct PassLoopKey {
@@ -393,6 +524,80 @@ cudaError_t loop_pool_bfs2d(PassLoop* L, const PoolBFS& p, int K, unsigned long 
   LF_BFS2D(4, 8) LF_BFS2D(4, 16) LF_BFS2D(4, 32) LF_BFS2D(8, 8) LF_BFS2D(8, 16) LF_BFS2D(8, 32)
 #undef LF_BFS2D
   return cudaErrorInvalidValue;
+}
+
+cudaError_t pool_pr2d(PassLoop* L, const void* maps, const PoolPR<int>& p, int TB, int variant,
+                      unsigned long long* fault, int tiles, int* ctl, unsigned cap,
+                      unsigned long long* passes, cudaStream_t s) {
+  int grid = 0, threads = TB * 32;
+  void* kern = nullptr;
+  size_t smem = 0;
+#define LF_PP(BB)                                                                    \
+  if (TB == BB) {                                                                    \
+    kern = variant == 1 ? kt_pool_setup<BB, 32>(grid) : kt_pool_setup<BB, 40>(grid); \
+    smem = PR2dPoolLayout<BB>::smem_bytes;                                           \
+  }
+  LF_PP(8) LF_PP(16) LF_PP(32)
+#undef LF_PP
+  if (!kern) return cudaErrorInvalidValue;
+  grid = std::max(1, std::min(grid, tiles));
+  const CUtensorMap* m = static_cast<const CUtensorMap*>(maps);
+  if (!L) {
+    const int* no_ctl = nullptr;
+    void* kargs[] = {&m, const_cast<PoolPR<int>*>(&p), &fault, &no_ctl};
+    return cudaLaunchKernel(kern, dim3(grid), dim3(threads), kargs, smem, s);
+  }
+  PassLoopKey key{};
+  int i = 0;
+  key.v[i++] = 3;  // push/relabel over a pool
+  key_common(key, i, p.q, p.inst0.g, p.inst, p.counters, fault, ctl, cap, 0, TB, grid);
+  key.v[i++] = variant;
+  key.v[i++] = p.sweeps;
+  key.v[i++] = (long long)(uintptr_t)m;
+  key.v[i++] = (long long)(uintptr_t)p.res;
+  key.v[i++] = (long long)(uintptr_t)p.exc;
+  key.v[i++] = (long long)(uintptr_t)p.h;
+  key.v[i++] = (long long)(uintptr_t)p.tile_inst;
+  const int* cp = ctl;
+  void* kargs[] = {&m, const_cast<PoolPR<int>*>(&p), &fault, &cp};
+  return run_loop(L, key, kern, grid, threads, smem, kargs, p.q, ctl, cap, passes, nullptr, s);
+}
+
+cudaError_t pool_bfs2d(PassLoop* L, const void* maps, const PoolBFS& p, int TB,
+                       unsigned long long* fault, int tiles, int* ctl, unsigned cap,
+                       unsigned long long* passes, unsigned long long* overflow, cudaStream_t s) {
+  int grid = 0, threads = TB * 32;
+  void* kern = nullptr;
+  size_t smem = 0;
+#define LF_PB(BB)                              \
+  if (TB == BB) {                              \
+    kern = bfs_kt_pool_setup<BB>(grid);        \
+    smem = BFS2dLayout<BB>::smem_bytes;        \
+  }
+  LF_PB(8) LF_PB(16) LF_PB(32)
+#undef LF_PB
+  if (!kern) return cudaErrorInvalidValue;
+  grid = std::max(1, std::min(grid, tiles));
+  const CUtensorMap* m = static_cast<const CUtensorMap*>(maps);
+  if (!L) {
+    const int* no_ctl = nullptr;
+    void* kargs[] = {&m, const_cast<PoolBFS*>(&p), &fault, &no_ctl};
+    return cudaLaunchKernel(kern, dim3(grid), dim3(threads), kargs, smem, s);
+  }
+  PassLoopKey key{};
+  int i = 0;
+  key.v[i++] = 4;  // BFS over a pool
+  key_common(key, i, p.q, p.inst0.g, p.inst, p.counters, fault, ctl, cap, 0, TB, grid);
+  key.v[i++] = p.max_local;
+  key.v[i++] = (long long)(uintptr_t)m;
+  key.v[i++] = (long long)(uintptr_t)p.h;
+  key.v[i++] = (long long)(uintptr_t)p.mask;
+  key.v[i++] = (long long)(uintptr_t)p.any_changed;
+  key.v[i++] = (long long)(uintptr_t)p.tile_inst;
+  key.v[i++] = (long long)(uintptr_t)overflow;
+  const int* cp = ctl;
+  void* kargs[] = {&m, const_cast<PoolBFS*>(&p), &fault, &cp};
+  return run_loop(L, key, kern, grid, threads, smem, kargs, p.q, ctl, cap, passes, overflow, s);
 }
 
 cudaError_t launch_pool_bfs2d(const PoolBFS& p, int K, unsigned long long* fault, int tiles,

@@ -65,6 +65,43 @@ struct PR2dMaps {
   CUtensorMap h;
 };
 
+// Where a lattice lives in the pools, as the 2-d passes need it.
+struct Lat2d {
+  int ntc, ntb, Cp;  // tiles per tile row, tile rows, padded row length
+  long long plane;   // elements between two of its residual planes
+  long long node_base, res_base;
+  int tile_base;
+};
+
+// The same fields of a lattice alone in its pool, read from its geometry
+// (kernel parameters) where they are needed; every base is 0.
+__device__ __forceinline__ int lat_ntc(const Geo& g) { return g.ntc; }
+__device__ __forceinline__ int lat_ntb(const Geo& g) { return g.ntb; }
+__device__ __forceinline__ int lat_Cp(const Geo& g) { return g.Cp; }
+__device__ __forceinline__ long long lat_plane(const Geo& g) { return g.NP; }
+__device__ __forceinline__ long long lat_node_base(const Geo&) { return 0; }
+__device__ __forceinline__ long long lat_res_base(const Geo&) { return 0; }
+__device__ __forceinline__ int lat_tile_base(const Geo&) { return 0; }
+__device__ __forceinline__ int lat_ntc(const Lat2d& L) { return L.ntc; }
+__device__ __forceinline__ int lat_ntb(const Lat2d& L) { return L.ntb; }
+__device__ __forceinline__ int lat_Cp(const Lat2d& L) { return L.Cp; }
+__device__ __forceinline__ long long lat_plane(const Lat2d& L) { return L.plane; }
+__device__ __forceinline__ long long lat_node_base(const Lat2d& L) { return L.node_base; }
+__device__ __forceinline__ long long lat_res_base(const Lat2d& L) { return L.res_base; }
+__device__ __forceinline__ int lat_tile_base(const Lat2d& L) { return L.tile_base; }
+
+__device__ __forceinline__ Lat2d lat2d_of(const InstDesc& I) {
+  Lat2d L;
+  L.ntc = I.g.ntc;
+  L.ntb = I.g.ntb;
+  L.Cp = I.g.Cp;
+  L.plane = I.plane;
+  L.node_base = I.node_base;
+  L.res_base = I.res_base;
+  L.tile_base = I.tile_base;
+  return L;
+}
+
 template <int K, int TB>
 struct PR2dLayout {
   static constexpr int NT = TB * 32;
@@ -150,21 +187,23 @@ __device__ __forceinline__ void pr2d_issue(const PR2dMaps& maps, const Geo& g, i
 // before the barrier that opens the visit (once a visit runs, neighbours
 // push into s_exc at once, and a later read would miss the flow they sent,
 // which the delta write-back of the excess needs).
-template <int K, int TB>
-__device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const Geo& g, int hmax, int cur,
-                                          unsigned char* stage, int tile, const int e0,
-                                          int my_h) {
-  using Ly = PR2dLayout<K, TB>;
-  constexpr int NT = Ly::NT;
+//
+// LAT: Lat2d for a lattice that is one of many in the pools (its nodes,
+// residual planes and tiles start at its bases; tile ids in the queue are
+// global), Geo for a lattice alone in its pool (all bases 0).
+template <int K, int TB, class LAT>
+__device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const LAT& L, int hmax, int cur,
+                                          int* s_res, int* s_exc, int* s_h, int tile,
+                                          const int e0, int my_h) {
+  constexpr int NT = TB * 32;
   constexpr int HW = kPr2dHaloW;
-  int* s_res = reinterpret_cast<int*>(stage);
-  int* s_exc = reinterpret_cast<int*>(stage + Ly::res_bytes);
-  int* s_h = reinterpret_cast<int*>(stage + Ly::res_bytes + Ly::exc_bytes);
   const int t = threadIdx.x;
   const int ic = t & 31, ib = t >> 5;
-  const int tc = tile % g.ntc, tb = tile / g.ntc;
+  const int tc = tile % lat_ntc(L), tb = tile / lat_ntc(L);
   const int b0 = tb * TB, c0 = tc * 32;
-  const long long gi = (long long)(b0 + ib) * g.Cp + (c0 + ic);
+  const long long gi = (long long)(b0 + ib) * lat_Cp(L) + (c0 + ic) + lat_node_base(L);
+  int* const res = p.res + (lat_res_base(L) - lat_node_base(L));  // res + k plane + gi
+  const int tile_g = lat_tile_base(L) + tile;
   const int hidx = (ib + 1) * HW + (ic + 4);
   const int nxt = cur ^ 1;
   // directions that leave the tile
@@ -198,16 +237,16 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const Geo& g, in
           s_res[rk * NT + tn] += d;
         } else {
           // across the tile edge: delivered at once with global atomics
-          int* r0 = p.res + gi;
-          atomicAdd(r0 + (long long)k * g.NP, -d);
-          const long long dn = (long long)s2_db<K>(k) * g.Cp + s2_dc<K>(k);
-          atomicAdd(r0 + (long long)rk * g.NP + dn, d);
+          int* r0 = res + gi;
+          atomicAdd(r0 + (long long)k * lat_plane(L), -d);
+          const long long dn = (long long)s2_db<K>(k) * lat_Cp(L) + s2_dc<K>(k);
+          atomicAdd(r0 + (long long)rk * lat_plane(L) + dn, d);
           atomicAdd(p.exc + gi + dn, d);
           // the neighbour's tile: one tile row / column over where the
           // neighbour leaves this tile's rows / columns
           const int dtb = (s2_db<K>(k) < 0 && ib == 0) ? -1 : (s2_db<K>(k) > 0 && ib == TB - 1) ? 1 : 0;
           const int dtc = (s2_dc<K>(k) < 0 && ic == 0) ? -1 : (s2_dc<K>(k) > 0 && ic == 31) ? 1 : 0;
-          enqueue_tile(p.q, nxt, tile + dtb * g.ntc + dtc);
+          enqueue_tile(p.q, nxt, tile_g + dtb * lat_ntc(L) + dtc);
         }
       }
       if (sent) atomicAdd(&s_exc[t], -sent);
@@ -238,13 +277,13 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const Geo& g, in
   else p.exc[gi] = ef;
 #pragma unroll
   for (int k = 0; k < K; ++k)  // edges across the tile edge were updated by their pushes
-    if (!((outm >> k) & 1u)) p.res[(long long)k * g.NP + gi] = s_res[k * NT + t];
+    if (!((outm >> k) & 1u)) res[(long long)k * lat_plane(L) + gi] = s_res[k * NT + t];
   p.h[gi] = my_h;
   // the buffer's next contents come from the async proxy: order this
   // visit's shared-memory accesses before them
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   const int still = ef > 0 && my_h < hmax;
-  if (__syncthreads_or(still) && t == 0) enqueue_tile(p.q, nxt, tile);
+  if (__syncthreads_or(still) && t == 0) enqueue_tile(p.q, nxt, tile_g);
 }
 
 // One lattice (the pool of one), no section mask, 32-bit capacities.
@@ -311,7 +350,111 @@ __global__ void __maxnreg__(REGS)
       if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
       return;
     }
-    pr2d_tile<K, TB>(p, g, hmax, cur, st, gt, e0, h0);
+    pr2d_tile<K, TB>(p, g, hmax, cur, reinterpret_cast<int*>(st),
+                            reinterpret_cast<int*>(st + Ly::res_bytes),
+                            reinterpret_cast<int*>(st + Ly::res_bytes + Ly::exc_bytes), gt, e0, h0);
+  }
+}
+
+// ------------------------------------------------------------ pools
+
+// Stage layout of the pool pass: room for 8 residual planes whatever the
+// tile's lattice has, so the excess and heights sit at fixed offsets.
+template <int TB>
+struct PR2dPoolLayout {
+  static constexpr int NT = TB * 32;
+  static constexpr int res_bytes = 8 * NT * 4;
+  static constexpr int exc_off = res_bytes;
+  static constexpr int h_off = exc_off + NT * 4;
+  static constexpr int h_bytes = (TB + 2) * kPr2dHaloW * 4;
+  static constexpr int stage_bytes = (h_off + h_bytes + 127) / 128 * 128;
+  static constexpr int smem_bytes = 2 * stage_bytes + 16 + 128;
+};
+
+// A lattice's three tensor maps (residual planes, excess, heights) in the
+// pool's map array (global memory, written before the launch).
+template <int TB>
+__device__ __forceinline__ void pr2d_pool_issue(const PoolPR<int>& p, const CUtensorMap* maps,
+                                                int gt, unsigned stage, unsigned bar) {
+  using Ly = PR2dPoolLayout<TB>;
+  const int ii = p.tile_inst[gt];
+  const InstDesc& I = p.inst[ii];
+  const int K = I.st.K;
+  const int tile = gt - I.tile_base;
+  const int tc = tile % I.g.ntc, tb = tile / I.g.ntc;
+  const int b0 = tb * TB, c0 = tc * 32;
+  mbar_expect_tx(bar, K * Ly::NT * 4 + Ly::NT * 4 + Ly::h_bytes);
+  tma_load_3d(stage, &maps[3 * ii], c0, b0, 0, bar);
+  tma_load_2d(stage + Ly::exc_off, &maps[3 * ii + 1], c0, b0, bar);
+  tma_load_2d(stage + Ly::h_off, &maps[3 * ii + 2], c0 - 4, b0 - 1, bar);
+}
+
+// Many 2-d lattices (Full2d_4 / Full2d_8, one tile height) in one pool,
+// 32-bit capacities, no section mask: the same pass as k_pool_pr2d, each
+// tile with its own lattice's placement, stencil, height cap and tensor
+// maps.  ctl as for k_pool_pr2d (the height caps and finished flags always
+// come from the descriptors in device memory).
+template <int TB, int REGS>
+__global__ void __maxnreg__(REGS)
+    k_pool_pr2d_pool(const CUtensorMap* maps, PoolPR<int> p, unsigned long long* fault,
+                     const int* ctl) {
+  using Ly = PR2dPoolLayout<TB>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<unsigned long long>(smem_raw) + 127) & ~127ull);
+  const unsigned bar0 = smem_addr(smem + 2 * Ly::stage_bytes);
+  const unsigned stage0 = smem_addr(smem);
+  const int cur = ctl ? *ctl : p.cur;
+  const unsigned n = queued_count(p.q, cur);
+  const int* list = p.q.list[cur];
+  if (blockIdx.x >= n) return;
+  if (threadIdx.x == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar0 + 8, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) pr2d_pool_issue<TB>(p, maps, list[blockIdx.x], stage0, bar0);
+  unsigned phases = 0;
+  unsigned buf = 0;
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x, buf ^= 1) {
+    const int gt = list[i];
+    if (threadIdx.x == 0) {
+      p.q.flag[cur][gt] = 0;
+      atomicAdd(&p.counters[0], 1ull);
+    }
+    const unsigned nx = i + gridDim.x;
+    if (threadIdx.x == 0 && nx < n)
+      pr2d_pool_issue<TB>(p, maps, list[nx], stage0 + (buf ^ 1) * Ly::stage_bytes,
+                          bar0 + (buf ^ 1) * 8);
+    const unsigned bar = bar0 + buf * 8;
+    const unsigned par = (phases >> buf) & 1u;
+    const bool ok = mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+    phases ^= 1u << buf;
+    unsigned char* st = smem + buf * Ly::stage_bytes;
+    int* s_res = reinterpret_cast<int*>(st);
+    int* s_exc = reinterpret_cast<int*>(st + Ly::exc_off);
+    int* s_h = reinterpret_cast<int*>(st + Ly::h_off);
+    // this node's staged excess and height (see pr2d_tile)
+    const int e0 = s_exc[threadIdx.x];
+    const int h0 = s_h[((threadIdx.x >> 5) + 1) * kPr2dHaloW + (threadIdx.x & 31) + 4];
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicExch(fault, 1ull);
+      mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+      if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
+      return;
+    }
+    const InstDesc& I = p.inst[p.tile_inst[gt]];
+    if (I.done) {  // the whole block reads the same flag
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      continue;
+    }
+    const Lat2d L = lat2d_of(I);
+    const int tile = gt - L.tile_base;
+    if (I.st.K == 8)
+      pr2d_tile<8, TB>(p, L, I.hmax, cur, s_res, s_exc, s_h, tile, e0, h0);
+    else
+      pr2d_tile<4, TB>(p, L, I.hmax, cur, s_res, s_exc, s_h, tile, e0, h0);
   }
 }
 

@@ -106,6 +106,26 @@ cudaError_t loop_pool_bfs2d(PassLoop* L, const PoolBFS& p, int K, unsigned long 
                             int tiles, int* ctl, unsigned cap, unsigned long long* passes,
                             unsigned long long* overflow, cudaStream_t s);
 
+// The same passes over a pool of many 2-d lattices (Full2d_4 / Full2d_8 mixed,
+// one tile height): pool2d_tile_rows gives that tile height, or 0 when the
+// pool does not fit them.  The tensor maps of every lattice live in device
+// memory (PoolMaps, rebuilt when the arrays move).  L: null for one launch
+// (p.cur), else a device-side loop of passes as above.
+struct PoolMaps;
+PoolMaps* pool_maps_new();
+void pool_maps_free(PoolMaps* m);
+int pool2d_tile_rows(const std::vector<InstDesc>& insts);
+const void* pool_maps_pr(PoolMaps* M, const std::vector<InstDesc>& insts, int* res, int* exc,
+                         int* h, cudaStream_t s);
+const void* pool_maps_bfs(PoolMaps* M, const std::vector<InstDesc>& insts, int* h,
+                          const uint64_t* mask, cudaStream_t s);
+cudaError_t pool_pr2d(PassLoop* L, const void* maps, const PoolPR<int>& p, int TB, int variant,
+                      unsigned long long* fault, int tiles, int* ctl, unsigned cap,
+                      unsigned long long* passes, cudaStream_t s);
+cudaError_t pool_bfs2d(PassLoop* L, const void* maps, const PoolBFS& p, int TB,
+                       unsigned long long* fault, int tiles, int* ctl, unsigned cap,
+                       unsigned long long* passes, unsigned long long* overflow, cudaStream_t s);
+
 cudaError_t launch_pool_bfs(const PoolBFS& p, int KA, int KB, bool single, int grid, int threads,
                             size_t smem, cudaStream_t s);
 cudaError_t launch_pool_reach(const PoolReach& p, int KA, int KB, bool single, int grid,
@@ -181,6 +201,7 @@ class PoolRunner {
   int* d_ctl = nullptr;                      // control words of the device-side loops
   PassLoop* loop_pr = nullptr;
   PassLoop* loop_bfs = nullptr;
+  PoolMaps* pool_maps = nullptr;  // tensor maps of the pool passes (batches)
   void* h_pin = nullptr;
   int threads = 1, hv_max = 0;
   int ka = 0, kb = 0;  // kernel sizes present in the pool

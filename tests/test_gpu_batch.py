@@ -88,3 +88,34 @@ def test_batch_3d_and_errors(native, gpu, oracle_port):
     B2.add("Full2d_8", (8, 8))
     with pytest.raises(ValueError):
         B2.add("Star2d_16", (8, 8))    # at most two kernel sizes
+
+
+@pytest.mark.parametrize("pr_kernel,bfs_kernel,host_loops", [(0, 0, 0), (0, 0, 1), (1, 1, 1), (2, 0, 0)])
+@pytest.mark.parametrize("tile_rows", [8, 16, 32])
+def test_batch_pass_variants(native, gpu, oracle_port, pr_kernel, bfs_kernel, host_loops, tile_rows):
+    """A pool of mixed 4- and 8-connected lattices through the TMA-staged pool
+    passes (device-side loops or one launch per pass) and the generic tile
+    passes: every lattice gets the oracle's energy and both cut sets."""
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    shapes = W.batch_shapes(20, seed=7 + tile_rows, lo=24, hi=260)
+    probs = [W.plain_cut(1200 + i, s, "Full2d_8" if i % 3 else "Full2d_4") for i, s in enumerate(shapes)]
+    B = lf.LatticeBatch()
+    for p in probs:
+        B.add(p.kernel, p.dims)
+    B.setParam("pr_kernel", pr_kernel)
+    B.setParam("bfs_kernel", bfs_kernel)
+    B.setParam("host_loops", host_loops)
+    B.setParam("tile_rows", tile_rows)
+    B.setParam("local_sweeps", 2)
+    B.setParam("launches_per_relabel", 4)
+    for i, p in enumerate(probs):
+        B.addCapacities(i, p.source, p.sink, p.edge)
+    for rep in range(2):
+        B.run()
+        for i, p in enumerate(probs):
+            u, b = p.energies()
+            E, cmin, cmax, _, _ = oracle_port.port_canonical(p.kernel, p.dims, u, b)
+            assert B.flow(i)[1] == E, (rep, i)
+            assert np.array_equal(B.getCut(i), cmin), (rep, i)
+            assert np.array_equal(B.getCutMax(i), cmax), (rep, i)
