@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--profile-run", action="store_true",
                     help="only warm-up and timed device-resident solves (for ncu captures)")
+    ap.add_argument("--host-loops", action="store_true",
+                    help="one launch per pass instead of device-side pass loops (CUDA graphs with "
+                         "conditional nodes, whose kernels a profiler does not list); same kernels")
     ap.add_argument("--tuning", default=None,
                     help="tile_rows,local_sweeps,launches_per_relabel instead of the autotuner "
                          "(e.g. the setting a bench run chose, for a profile run)")
@@ -258,6 +261,8 @@ def run_ours(args):
 
     tuning = None
     tune_table = None
+    if args.host_loops:
+        L.setParam("host_loops", 1)
     if args.tuning:
         tr_, sw_, lp_ = (int(x) for x in args.tuning.split(","))
         tuning = {"tile_rows": tr_, "local_sweeps": sw_, "launches_per_relabel": lp_}
@@ -303,13 +308,19 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     pr_bytes = prof["pr_tiles"] * nt * 2 * (K * elem + elem + 4)
     bfs_bytes = prof["bfs_tiles"] * nt * (8 + 4 + 4)
+    # a single 2-d lattice with a 3x3 stencil runs the TMA-staged passes
+    # (k_pool_pr2d for 32-bit capacities, k_pool_bfs2d for any); other
+    # lattices the generic tile kernels
+    tma2d = p.kernel in ("Full2d_4", "Full2d_8") and len(p.dims) == 2
+    pr_name = "k_pool_pr2d" if tma2d and elem == 4 else "k_pool_pr"
+    bfs_name = "k_pool_bfs2d" if tma2d else "k_pool_bfs"
     if prof["pr_ms"] >= prof["bfs_ms"]:
-        kname, kbytes, kms, klaunch = "k_pool_pr", pr_bytes, prof["pr_ms"], prof["pr_launches"]
+        kname, kbytes, kms, klaunch = pr_name, pr_bytes, prof["pr_ms"], prof["pr_launches"]
     else:
-        kname, kbytes, kms, klaunch = "k_pool_bfs", bfs_bytes, prof["bfs_ms"], prof["bfs_passes"]
+        kname, kbytes, kms, klaunch = bfs_name, bfs_bytes, prof["bfs_ms"], prof["bfs_passes"]
     achieved = kbytes / (kms * 1e-3) / 1e9 if kms > 0 else 0.0
     tr = committed_traffic("%s:%s:%s" % (args.workload, kname, "x".join(str(v) for v in tile)))
-    klaunch_nodes = (prof["pr_tiles"] if kname == "k_pool_pr" else prof["bfs_tiles"]) * nt / max(1, klaunch)
+    klaunch_nodes = (prof["pr_tiles"] if kname.startswith("k_pool_pr") else prof["bfs_tiles"]) * nt / max(1, klaunch)
     roofline = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs, copy)",

@@ -18,6 +18,10 @@ namespace lfg {
 //   node cost A (off) / D (on), then f(0,1) = B - A, f(1,0) = C - D as two
 //   directed capacities, moving a negative one into the unary terms.
 // exc = cost(off) - cost(on): > 0 prefers on (supply), < 0 prefers off.
+// VEC: the caller's arrays are 16-byte aligned, so each pairwise table (32
+// bytes) is read with two 16-byte loads and each unary pair with one; fewer,
+// wider requests matter when the arrays are pinned host memory read in place.
+template <bool VEC>
 __global__ void k_fill_energy(Geo g, Stencil st, int nd, long long N, const int64_t* unary,
                               const int64_t* binary, long long* exc, long long* cap,
                               long long* c0sum, int* err) {
@@ -33,7 +37,15 @@ __global__ void k_fill_energy(Geo g, Stencil st, int nd, long long N, const int6
     else { c = int(b % g.C); bb = int((b / g.C) % g.B); a = int(b / ((long long)g.C * g.B)); }
     long long u = ((long long)a * g.Bp + bb) * g.Cp + c;
     if (e == 0) {
-      int64_t E0 = unary[2 * b], E1 = unary[2 * b + 1];
+      int64_t E0, E1;
+      if (VEC) {
+        const longlong2 ue = reinterpret_cast<const longlong2*>(unary)[b];
+        E0 = ue.x;
+        E1 = ue.y;
+      } else {
+        E0 = unary[2 * b];
+        E1 = unary[2 * b + 1];
+      }
       atom_add(&exc[u], (long long)(E0 - E1));
       c0 += E0;
     }
@@ -41,7 +53,14 @@ __global__ void k_fill_energy(Geo g, Stencil st, int nd, long long N, const int6
     if (na >= 0 && na < g.A && nb >= 0 && nb < g.B && nc >= 0 && nc < g.C) {
       long long v = ((long long)na * g.Bp + nb) * g.Cp + nc;
       const int64_t* q = binary + (b * Kp + e) * 4;
-      long long A = q[0], B = q[1], C = q[2], D = q[3];
+      long long A, B, C, D;
+      if (VEC) {
+        const longlong2 q0 = reinterpret_cast<const longlong2*>(q)[0];
+        const longlong2 q1 = reinterpret_cast<const longlong2*>(q)[1];
+        A = q0.x; B = q0.y; C = q1.x; D = q1.y;
+      } else {
+        A = q[0]; B = q[1]; C = q[2]; D = q[3];
+      }
       c0 += A;
       long long du = A - D, dv = 0;
       long long Bq = B - A, Cq = C - D;
@@ -244,7 +263,11 @@ cudaError_t launch_fill_energy(const Geo& g, const Stencil& st, int nd, long lon
                                const int64_t* u, const int64_t* b, long long* exc,
                                long long* cap, long long* c0, int* err, cudaStream_t s) {
   long long n = N * (st.K / 2);
-  if (n > 0) k_fill_energy<<<nblk(n, 256), 256, 0, s>>>(g, st, nd, N, u, b, exc, cap, c0, err);
+  const bool vec = (reinterpret_cast<uintptr_t>(u) % 16 == 0) && (reinterpret_cast<uintptr_t>(b) % 16 == 0);
+  if (n > 0) {
+    if (vec) k_fill_energy<true><<<nblk(n, 256), 256, 0, s>>>(g, st, nd, N, u, b, exc, cap, c0, err);
+    else k_fill_energy<false><<<nblk(n, 256), 256, 0, s>>>(g, st, nd, N, u, b, exc, cap, c0, err);
+  }
   return cudaGetLastError();
 }
 

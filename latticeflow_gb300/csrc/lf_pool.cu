@@ -546,7 +546,7 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
                           d_counters + 5, d_counters + 7, stream),
           "bfs loop (TMA)");
     mark(1, true);
-    count_launch();
+    // kernels of the loop are counted from its pass counter
     return;
   }
   // a pool of 2-d lattices: the TMA-staged pass with each lattice's maps
@@ -564,7 +564,7 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
                      d_counters + 5, d_counters + 7, stream),
           "bfs loop (TMA, pool)");
     mark(1, true);
-    count_launch();
+    // kernels of the loop are counted from its pass counter
     return;
   }
   int cur = 0;
@@ -709,7 +709,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
                         std::max(tiles, 1), d_ctl, (unsigned)M, d_counters + 6, stream),
               "push-relabel loop (TMA, pool)");
         mark(0, true);
-        count_launch();
+        // kernels of the loop are counted from its pass counter
         drain_queue();
         continue;
       }
@@ -721,7 +721,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
                              std::max(tiles, 1), d_ctl, (unsigned)M, d_counters + 6, stream),
               "push-relabel loop (TMA)");
         mark(0, true);
-        count_launch();
+        // kernels of the loop are counted from its pass counter
         drain_queue();
         continue;
       }
@@ -762,6 +762,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   stats.bfs_tiles += c[1];
   stats.bfs_passes += (long long)c[5];
   stats.pr_launches += (long long)c[6];
+  if (hooks) hooks->launches += 2 * (long long)(c[5] + c[6]);  // pass + control kernel per pass
   if (c[4]) throw LfError{6, "a tile's staging copy did not complete in time"};
   if (c[7]) throw LfError{4, "global relabel did not converge"};
 }

@@ -298,3 +298,32 @@ def test_tma_pass_full_size_all_variants(native, gpu, oracle_port):
             assert (flow, energy) == ref[:2], (prk, rows)
             assert np.array_equal(cmin, ref[2]) and np.array_equal(cmax, ref[3]), (prk, rows)
         del L
+
+
+def test_unaligned_energy_arrays(native, gpu, oracle_port):
+    """Device energy arrays that are 8- but not 16-byte aligned take the
+    scalar fill (aligned ones the 16-byte vector fill); both give the
+    oracle's answer."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import _native as N
+    from latticeflow_gb300 import workloads as W
+    p = W.plain_cut(44, (90, 110), "Full2d_8")
+    u, b = p.energies()
+    E, cmin, cmax, _, _ = oracle_port.port_canonical(p.kernel, p.dims, u, b)
+    for off in (0, 1):
+        ub = torch.zeros(u.size + 2, dtype=torch.int64, device="cuda")
+        bb = torch.zeros(b.size + 2, dtype=torch.int64, device="cuda")
+        uu = ub[off:off + u.size]
+        bv = bb[off:off + b.size]
+        uu.copy_(torch.from_numpy(u.reshape(-1)))
+        bv.copy_(torch.from_numpy(b.reshape(-1)))
+        assert (uu.data_ptr() % 16 == 0) == (off == 0) and (bv.data_ptr() % 16 == 0) == (off == 0)
+        torch.cuda.synchronize()
+        L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+        N.check(N.lib().lf_add_energy_potentials_device(L._h, ctypes.c_void_p(uu.data_ptr()),
+                                                        ctypes.c_void_p(bv.data_ptr())))
+        L.run()
+        assert L.flow()[1] == E
+        assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
