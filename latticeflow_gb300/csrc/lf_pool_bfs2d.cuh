@@ -92,8 +92,13 @@ __device__ __forceinline__ void bfs2d_tile(const PoolBFS& p, const LAT& L, int c
         best = hn < best ? hn : best;
       }
     }
-    best = row_scan_from_left(best, can_l, ic);
-    best = row_scan_from_right(best, can_r, ic);
+    // after the first iteration the row is consistent along its row edges
+    // (each node at most one above a neighbour it can push to), and stays so
+    // while no node of the row improves: the scans change nothing then
+    if (it == 0 || __any_sync(0xffffffffu, best < my_h)) {
+      best = row_scan_from_left(best, can_l, ic);
+      best = row_scan_from_right(best, can_r, ic);
+    }
     const int c = best < my_h;
     if (c) {
       my_h = best;

@@ -96,9 +96,13 @@ __device__ __forceinline__ void bfs_tile(const PoolBFS& p, const InstDesc& I, Po
         best = hn < best ? hn : best;
       }
     }
-    // whole rows at once: every lane of the warp takes part
-    if (kl >= 0) best = row_scan_from_left(best, can_l, lane);
-    if (kr >= 0) best = row_scan_from_right(best, can_r, lane);
+    // whole rows at once: every lane of the warp takes part (after the first
+    // iteration a row is consistent along its row edges and stays so while
+    // none of its nodes improves: the scans change nothing then)
+    if (it == 0 || __any_sync(0xffffffffu, best < my_h)) {
+      if (kl >= 0) best = row_scan_from_left(best, can_l, lane);
+      if (kr >= 0) best = row_scan_from_right(best, can_r, lane);
+    }
     const int c = best < my_h;
     if (c) {
       my_h = best;

@@ -269,9 +269,12 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const LAT& L, in
       }
       act = my_h < hmax;
     }
+    // after the last sweep no vote and no barrier: the write-back below
+    // reads only this node's own excess and residuals, final since the
+    // barrier after the push phase (the relabel phase writes heights only)
+    if (it + 1 == p.sweeps) break;
     if (!__syncthreads_or(act)) break;
   }
-  __syncthreads();
   const int ef = s_exc[t];
   if (outm) atomicAdd(&p.exc[gi], ef - e0);
   else p.exc[gi] = ef;

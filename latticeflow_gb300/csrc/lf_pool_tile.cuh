@@ -142,9 +142,12 @@ __device__ void pr_tile(const PoolPR<T>& p, const InstDesc& I, PoolSmemHead* hd,
       }
       act = my_h < hmax;
     }
+    // after the last sweep no vote and no barrier: the write-back below
+    // reads only this node's own excess and residuals, final since the
+    // barrier after the push phase (the relabel phase writes heights only)
+    if (it + 1 == p.sweeps) break;
     if (!__syncthreads_or(act)) break;
   }
-  __syncthreads();
   int still = 0;
   if (live) {
     const T ef = s_exc[t];
