@@ -246,6 +246,9 @@ void engine_run_parametric(Engine& E) {
   // problems: 6.7x fewer milliseconds at 1024^2 than the binary-cut setting).
   if (E.tune.sweeps <= 0) E.tune.sweeps = 16;
   if (E.tune.launches_per_relabel <= 0) E.tune.launches_per_relabel = 64;
+  // 16-row tiles: with the TMA-staged 64-bit pass, 1024^2 TV solves ran
+  // 10-20% faster than with 32-row tiles (lambda 1e-3 and 0.05)
+  if (E.tune.tile_rows <= 0) E.tune.tile_rows = 16;
   // Tail step only when a single node is still active, with trees as large
   // as a section: after a generation's flow the remainder can sit in one
   // node beside a million nodes short of one unit each, which the tile

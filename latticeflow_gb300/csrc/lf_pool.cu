@@ -692,6 +692,36 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
         continue;
       }
     }
+    if constexpr (std::is_same<T, long long>::value) {
+      // 64-bit capacities with section masks on one 2-d lattice (parametric /
+      // TV section solves): the TMA-staged pass, in a device-side loop
+      PoolPR<long long> p{host[0], d_inst, d_tile_inst, res, exc, h, kmask, q, 0, R, d_counters};
+      const int k64 = tune.pr_kernel != 1 ? pr2d64_kernel_size(p, n == 1) : 0;
+      if (k64) {
+        if (!loop_pr) loop_pr = pass_loop_new();
+        mark(0, false);
+        if (tune.host_loops != 1) {
+          check(pr2d64(loop_pr, p, k64, d_counters + 4, std::max(tiles, 1), d_ctl, (unsigned)M,
+                       d_counters + 6, stream),
+                "push-relabel loop (TMA, 64-bit)");
+        } else {
+          int cur = 0;
+          for (int l = 0; l < M; ++l) {
+            prep_pass(cur);
+            p.cur = cur;
+            check(pr2d64(nullptr, p, k64, d_counters + 4, std::max(tiles, 1), nullptr, 0, nullptr,
+                         stream),
+                  "push-relabel pass (TMA, 64-bit)");
+            count_launch();
+            ++stats.pr_launches;
+            cur ^= 1;
+          }
+        }
+        mark(0, true);
+        drain_queue();
+        continue;
+      }
+    }
     const void* pmaps = nullptr;  // pool of 2-d lattices: the TMA-staged pass
     int tb_pool = 0;
     if constexpr (std::is_same<T, int>::value) {

@@ -113,6 +113,59 @@ cudaError_t launch_kt(const PR2dMaps& maps, const PoolPR<int>& p, unsigned long 
   return cudaGetLastError();
 }
 
+// Tensor maps of the 64-bit pass with section masks, cached per host thread.
+struct MapCache64 {
+  const void *res = nullptr, *exc = nullptr, *h = nullptr, *km = nullptr;
+  int Cp = 0, Bp = 0, K = 0, TB = 0;
+  long long NP = 0;
+  PR2dMaps64 maps;
+};
+
+bool maps64_for(const PoolPR<long long>& p, int K, int TB, PR2dMaps64& out) {
+  thread_local MapCache64 c;
+  const Geo& g = p.inst0.g;
+  if (c.res == p.res && c.exc == p.exc && c.h == p.h && c.km == p.kmask && c.Cp == g.Cp &&
+      c.Bp == g.Bp && c.NP == g.NP && c.K == K && c.TB == TB) {
+    out = c.maps;
+    return true;
+  }
+  PR2dMaps64 m;
+  const cuuint64_t d3[3] = {(cuuint64_t)g.Cp, (cuuint64_t)g.Bp, (cuuint64_t)K};
+  const cuuint64_t s3[2] = {(cuuint64_t)g.Cp * 8, (cuuint64_t)g.NP * 8};
+  const cuuint32_t b3[3] = {32, (cuuint32_t)TB, (cuuint32_t)K};
+  const cuuint64_t d2[2] = {(cuuint64_t)g.Cp, (cuuint64_t)g.Bp};
+  const cuuint64_t s8[1] = {(cuuint64_t)g.Cp * 8};
+  const cuuint64_t s4[1] = {(cuuint64_t)g.Cp * 4};
+  const cuuint32_t be[2] = {32, (cuuint32_t)TB};
+  const cuuint32_t bh[2] = {(cuuint32_t)kPr2dHaloW, (cuuint32_t)(TB + 2)};
+  if (!encode(&m.res, p.res, 3, d3, s3, b3, CU_TENSOR_MAP_DATA_TYPE_INT64) ||
+      !encode(&m.exc, p.exc, 2, d2, s8, be, CU_TENSOR_MAP_DATA_TYPE_INT64) ||
+      !encode(&m.h, p.h, 2, d2, s4, bh) ||
+      !encode(&m.km, const_cast<uint64_t*>(p.kmask), 2, d2, s8, be, CU_TENSOR_MAP_DATA_TYPE_UINT64))
+    return false;
+  c.res = p.res; c.exc = p.exc; c.h = p.h; c.km = p.kmask;
+  c.Cp = g.Cp; c.Bp = g.Bp; c.NP = g.NP; c.K = K; c.TB = TB;
+  c.maps = m;
+  out = m;
+  return true;
+}
+
+template <int K, int TB>
+void* kt64_setup(int& grid) {
+  using Ly = PR2dLayout64<K, TB>;
+  auto kern = k_pool_pr2d64<K, TB>;
+  static std::mutex mu;
+  static int cap = 0;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!cap) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Ly::smem_bytes);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cap = occupancy_grid(kern, Ly::NT, Ly::smem_bytes);
+  }
+  grid = cap;
+  return reinterpret_cast<void*>(kern);
+}
+
 // Tensor maps of the BFS pass (heights with halo, masks), cached like the
 // push/relabel ones.
 struct BfsMapCache {
@@ -524,6 +577,48 @@ cudaError_t loop_pool_bfs2d(PassLoop* L, const PoolBFS& p, int K, unsigned long 
   LF_BFS2D(4, 8) LF_BFS2D(4, 16) LF_BFS2D(4, 32) LF_BFS2D(8, 8) LF_BFS2D(8, 16) LF_BFS2D(8, 32)
 #undef LF_BFS2D
   return cudaErrorInvalidValue;
+}
+
+int pr2d64_kernel_size(const PoolPR<long long>& p, bool single) {
+  return p.kmask ? lattice2d_kernel_size(p.inst0, single) : 0;
+}
+
+// the 64-bit pass with section masks: one launch (L null, p.cur) or a
+// device-side loop of passes
+cudaError_t pr2d64(PassLoop* L, const PoolPR<long long>& p, int K, unsigned long long* fault,
+                   int tiles, int* ctl, unsigned cap, unsigned long long* passes, cudaStream_t s) {
+  PR2dMaps64 maps;
+  const int TB = p.inst0.g.TB;
+  if (!maps64_for(p, K, TB, maps)) return cudaErrorInvalidValue;
+  int grid = 0, threads = TB * 32;
+  void* kern = nullptr;
+  size_t smem = 0;
+#define LF_P64(KK, BB)                                  \
+  if (K == KK && TB == BB) {                            \
+    kern = kt64_setup<KK, BB>(grid);                    \
+    smem = PR2dLayout64<KK, BB>::smem_bytes;            \
+  }
+  LF_P64(4, 8) LF_P64(4, 16) LF_P64(4, 32) LF_P64(8, 8) LF_P64(8, 16) LF_P64(8, 32)
+#undef LF_P64
+  if (!kern) return cudaErrorInvalidValue;
+  grid = std::max(1, std::min(grid, tiles));
+  if (!L) {
+    const int* no_ctl = nullptr;
+    void* kargs[] = {&maps, const_cast<PoolPR<long long>*>(&p), &fault, &no_ctl};
+    return cudaLaunchKernel(kern, dim3(grid), dim3(threads), kargs, smem, s);
+  }
+  PassLoopKey key{};
+  int i = 0;
+  key.v[i++] = 5;  // 64-bit push/relabel with section masks
+  key_common(key, i, p.q, p.inst0.g, p.inst, p.counters, fault, ctl, cap, K, TB, grid);
+  key.v[i++] = p.sweeps;
+  key.v[i++] = (long long)(uintptr_t)p.res;
+  key.v[i++] = (long long)(uintptr_t)p.exc;
+  key.v[i++] = (long long)(uintptr_t)p.h;
+  key.v[i++] = (long long)(uintptr_t)p.kmask;
+  const int* cp = ctl;
+  void* kargs[] = {&maps, const_cast<PoolPR<long long>*>(&p), &fault, &cp};
+  return run_loop(L, key, kern, grid, threads, smem, kargs, p.q, ctl, cap, passes, nullptr, s);
 }
 
 cudaError_t pool_pr2d(PassLoop* L, const void* maps, const PoolPR<int>& p, int TB, int variant,

@@ -191,10 +191,15 @@ __device__ __forceinline__ void pr2d_issue(const PR2dMaps& maps, const Geo& g, i
 // LAT: Lat2d for a lattice that is one of many in the pools (its nodes,
 // residual planes and tiles start at its bases; tile ids in the queue are
 // global), Geo for a lattice alone in its pool (all bases 0).
-template <int K, int TB, class LAT>
-__device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const LAT& L, int hmax, int cur,
-                                          int* s_res, int* s_exc, int* s_h, int tile,
-                                          const int e0, int my_h) {
+//
+// T: capacity type (int for binary cuts, long long for parametric / TV
+// section solves); km: the node's staged section mask (bit k: direction k
+// stays inside the node's section), or null when the pass has none.
+template <int K, int TB, class LAT, class T = int>
+__device__ __forceinline__ void pr2d_tile(const PoolPR<T>& p, const LAT& L, int hmax, int cur,
+                                          T* s_res, T* s_exc, int* s_h, int tile,
+                                          const T e0, int my_h,
+                                          const uint64_t* s_km = nullptr) {
   constexpr int NT = TB * 32;
   constexpr int HW = kPr2dHaloW;
   const int t = threadIdx.x;
@@ -202,7 +207,8 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const LAT& L, in
   const int tc = tile % lat_ntc(L), tb = tile / lat_ntc(L);
   const int b0 = tb * TB, c0 = tc * 32;
   const long long gi = (long long)(b0 + ib) * lat_Cp(L) + (c0 + ic) + lat_node_base(L);
-  int* const res = p.res + (lat_res_base(L) - lat_node_base(L));  // res + k plane + gi
+  T* const res = p.res + (lat_res_base(L) - lat_node_base(L));  // res + k plane + gi
+  const uint64_t km = s_km ? s_km[t] : ~0ull;
   const int tile_g = lat_tile_base(L) + tile;
   const int hidx = (ib + 1) * HW + (ic + 4);
   const int nxt = cur ^ 1;
@@ -214,34 +220,35 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const LAT& L, in
     if (nb < 0 || nb >= TB || nc < 0 || nc >= 32) outm |= 1u << k;
   }
   for (int it = 0; it < p.sweeps; ++it) {
-    int e = s_exc[t];
+    T e = s_exc[t];
     // a node parked at the epoch cap no longer relabels but still pushes
     // downhill (a lower neighbour may be a deficit)
     if (e > 0) {
-      int sent = 0;
+      T sent = 0;
 #pragma unroll
       for (int k = 0; k < K; ++k) {
-        const int rem = e - sent;
+        const T rem = e - sent;
         if (rem <= 0) break;
-        const int r = s_res[k * NT + t];
+        if (!((km >> k) & 1)) continue;
+        const T r = s_res[k * NT + t];
         if (r <= 0) continue;
         if (s_h[hidx + s2_db<K>(k) * HW + s2_dc<K>(k)] >= my_h) continue;
-        const int d = rem < r ? rem : r;
+        const T d = rem < r ? rem : r;
         s_res[k * NT + t] = r - d;
         sent += d;
         constexpr int half = K / 2;
         const int rk = k < half ? k + half : k - half;
         if (!((outm >> k) & 1u)) {
           const int tn = t + s2_db<K>(k) * 32 + s2_dc<K>(k);
-          atomicAdd(&s_exc[tn], d);
+          atom_add(&s_exc[tn], d);
           s_res[rk * NT + tn] += d;
         } else {
           // across the tile edge: delivered at once with global atomics
-          int* r0 = res + gi;
-          atomicAdd(r0 + (long long)k * lat_plane(L), -d);
+          T* r0 = res + gi;
+          atom_add(r0 + (long long)k * lat_plane(L), (T)-d);
           const long long dn = (long long)s2_db<K>(k) * lat_Cp(L) + s2_dc<K>(k);
-          atomicAdd(r0 + (long long)rk * lat_plane(L) + dn, d);
-          atomicAdd(p.exc + gi + dn, d);
+          atom_add(r0 + (long long)rk * lat_plane(L) + dn, d);
+          atom_add(p.exc + gi + dn, d);
           // the neighbour's tile: one tile row / column over where the
           // neighbour leaves this tile's rows / columns
           const int dtb = (s2_db<K>(k) < 0 && ib == 0) ? -1 : (s2_db<K>(k) > 0 && ib == TB - 1) ? 1 : 0;
@@ -249,7 +256,7 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const LAT& L, in
           enqueue_tile(p.q, nxt, tile_g + dtb * lat_ntc(L) + dtc);
         }
       }
-      if (sent) atomicAdd(&s_exc[t], -sent);
+      if (sent) atom_add(&s_exc[t], (T)-sent);
     }
     __syncthreads();
     e = s_exc[t];
@@ -258,7 +265,7 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const LAT& L, in
       int hmin = kHInf;
 #pragma unroll
       for (int k = 0; k < K; ++k) {
-        if (s_res[k * NT + t] > 0) {
+        if (((km >> k) & 1) && s_res[k * NT + t] > 0) {
           const int hn = s_h[hidx + s2_db<K>(k) * HW + s2_dc<K>(k)];
           hmin = hn < hmin ? hn : hmin;
         }
@@ -275,8 +282,8 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<int>& p, const LAT& L, in
     if (it + 1 == p.sweeps) break;
     if (!__syncthreads_or(act)) break;
   }
-  const int ef = s_exc[t];
-  if (outm) atomicAdd(&p.exc[gi], ef - e0);
+  const T ef = s_exc[t];
+  if (outm) atom_add(&p.exc[gi], (T)(ef - e0));
   else p.exc[gi] = ef;
 #pragma unroll
   for (int k = 0; k < K; ++k)  // edges across the tile edge were updated by their pushes
@@ -356,6 +363,103 @@ __global__ void __maxnreg__(REGS)
     pr2d_tile<K, TB>(p, g, hmax, cur, reinterpret_cast<int*>(st),
                             reinterpret_cast<int*>(st + Ly::res_bytes),
                             reinterpret_cast<int*>(st + Ly::res_bytes + Ly::exc_bytes), gt, e0, h0);
+  }
+}
+
+// ------------------------------------------------ 64-bit, section mask
+
+// tensor maps of one lattice for the 64-bit pass: residual planes, excess
+// (int64), heights (int32), section masks (uint64)
+struct PR2dMaps64 {
+  CUtensorMap res;
+  CUtensorMap exc;
+  CUtensorMap h;
+  CUtensorMap km;
+};
+
+template <int K, int TB>
+struct PR2dLayout64 {
+  static constexpr int NT = TB * 32;
+  static constexpr int res_bytes = K * NT * 8;
+  static constexpr int exc_off = res_bytes;
+  static constexpr int h_off = exc_off + NT * 8;
+  static constexpr int h_bytes = (TB + 2) * kPr2dHaloW * 4;
+  static constexpr int km_off = (h_off + h_bytes + 127) / 128 * 128;
+  static constexpr int stage_bytes = km_off + NT * 8;
+  static constexpr int tx_bytes = res_bytes + NT * 8 + h_bytes + NT * 8;
+  static constexpr int smem_bytes = 2 * stage_bytes + 16 + 128;
+};
+
+template <int K, int TB>
+__device__ __forceinline__ void pr2d64_issue(const PR2dMaps64& maps, const Geo& g, int tile,
+                                             unsigned stage, unsigned bar) {
+  using Ly = PR2dLayout64<K, TB>;
+  const int tc = tile % g.ntc, tb = tile / g.ntc;
+  const int b0 = tb * TB, c0 = tc * 32;
+  mbar_expect_tx(bar, Ly::tx_bytes);
+  tma_load_3d(stage, &maps.res, c0, b0, 0, bar);
+  tma_load_2d(stage + Ly::exc_off, &maps.exc, c0, b0, bar);
+  tma_load_2d(stage + Ly::h_off, &maps.h, c0 - 4, b0 - 1, bar);
+  tma_load_2d(stage + Ly::km_off, &maps.km, c0, b0, bar);
+}
+
+// One lattice, 64-bit capacities, section mask (the parametric / TV section
+// solves): the pass of k_pool_pr2d with the mask staged beside the tile.
+template <int K, int TB>
+__global__ void __launch_bounds__(TB * 32)
+    k_pool_pr2d64(const __grid_constant__ PR2dMaps64 maps, PoolPR<long long> p,
+                  unsigned long long* fault, const int* ctl) {
+  using Ly = PR2dLayout64<K, TB>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<unsigned long long>(smem_raw) + 127) & ~127ull);
+  const unsigned bar0 = smem_addr(smem + 2 * Ly::stage_bytes);
+  const unsigned stage0 = smem_addr(smem);
+  const Geo& g = p.inst0.g;
+  const int cur = ctl ? *ctl : p.cur;
+  const unsigned n = queued_count(p.q, cur);
+  const int* list = p.q.list[cur];
+  if (blockIdx.x >= n) return;
+  const int hmax = ctl ? p.inst[0].hmax : p.inst0.hmax;
+  if (threadIdx.x == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar0 + 8, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const bool done = (ctl ? p.inst[0].done : p.inst0.done) != 0;
+  if (threadIdx.x == 0 && !done) pr2d64_issue<K, TB>(maps, g, list[blockIdx.x], stage0, bar0);
+  unsigned phases = 0;
+  unsigned buf = 0;
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x, buf ^= 1) {
+    const int gt = list[i];
+    if (threadIdx.x == 0) {
+      p.q.flag[cur][gt] = 0;
+      atomicAdd(&p.counters[0], 1ull);
+    }
+    if (done) continue;
+    const unsigned nx = i + gridDim.x;
+    if (threadIdx.x == 0 && nx < n)
+      pr2d64_issue<K, TB>(maps, g, list[nx], stage0 + (buf ^ 1) * Ly::stage_bytes,
+                          bar0 + (buf ^ 1) * 8);
+    const unsigned bar = bar0 + buf * 8;
+    const unsigned par = (phases >> buf) & 1u;
+    const bool ok = mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+    phases ^= 1u << buf;
+    unsigned char* st = smem + buf * Ly::stage_bytes;
+    long long* s_res = reinterpret_cast<long long*>(st);
+    long long* s_exc = reinterpret_cast<long long*>(st + Ly::exc_off);
+    int* s_h = reinterpret_cast<int*>(st + Ly::h_off);
+    const uint64_t* s_km = reinterpret_cast<const uint64_t*>(st + Ly::km_off);
+    const long long e0 = s_exc[threadIdx.x];  // before the opening barrier (see pr2d_tile)
+    const int h0 = s_h[((threadIdx.x >> 5) + 1) * kPr2dHaloW + (threadIdx.x & 31) + 4];
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicExch(fault, 1ull);
+      mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+      if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
+      return;
+    }
+    pr2d_tile<K, TB, Geo, long long>(p, g, hmax, cur, s_res, s_exc, s_h, gt, e0, h0, s_km);
   }
 }
 

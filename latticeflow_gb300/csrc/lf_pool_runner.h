@@ -106,6 +106,14 @@ cudaError_t loop_pool_bfs2d(PassLoop* L, const PoolBFS& p, int K, unsigned long 
                             int tiles, int* ctl, unsigned cap, unsigned long long* passes,
                             unsigned long long* overflow, cudaStream_t s);
 
+// The push/relabel pass for 64-bit capacities with section masks (parametric
+// and TV section solves) on one 2-d lattice: pr2d64_kernel_size gives the
+// kernel size it takes (0 when the pass does not fit it); pr2d64 runs one
+// launch (L null) or a device-side loop of passes.
+int pr2d64_kernel_size(const PoolPR<long long>& p, bool single);
+cudaError_t pr2d64(PassLoop* L, const PoolPR<long long>& p, int K, unsigned long long* fault,
+                   int tiles, int* ctl, unsigned cap, unsigned long long* passes, cudaStream_t s);
+
 // The same passes over a pool of many 2-d lattices (Full2d_4 / Full2d_8 mixed,
 // one tile height): pool2d_tile_rows gives that tile height, or 0 when the
 // pool does not fit them.  The tensor maps of every lattice live in device

@@ -87,3 +87,35 @@ def test_level_reductions_vs_oracle(native, gpu, oracle_port, kernel, dims):
     assert int(r.sum()) == int(r_ref.sum())      # total is exact
     sure = np.abs(r_ref) > R_TOL
     assert np.array_equal(L.getCut()[sure], cut_ref[sure])
+
+
+@pytest.mark.parametrize("kernel,dims", [("Full2d_4", (70, 66)), ("Full2d_8", (45, 52))])
+@pytest.mark.parametrize("pr_kernel,host_loops,tile_rows", [(0, 0, 8), (0, 0, 16), (0, 1, 32),
+                                                            (1, 0, 16), (1, 1, 32)])
+def test_level_reductions_pass_variants(native, gpu, oracle_port, kernel, dims, pr_kernel,
+                                        host_loops, tile_rows):
+    """Section solves through the TMA-staged 64-bit pass with section masks
+    (pr_kernel 0; device-side loops or one launch per pass) and the generic
+    tile pass (1): levels within one raw unit of the oracle, totals exact."""
+    import latticeflow_gb300 as lf
+    O = oracle_port
+    rng = np.random.default_rng(23)
+    offs, _ = O.lattice_offsets(kernel)
+    N, Kp = int(np.prod(dims)), len(offs) // 2
+    u = rng.integers(0, 5000, size=(N, 2)).astype(np.int64)
+    w = rng.integers(0, 900, size=(N, Kp)).astype(np.int64)
+    b = np.zeros((N, Kp, 4), np.int64)
+    b[:, :, 1] = w
+    b[:, :, 2] = w
+    r_ref, cut_ref, _ = O.port_pf(kernel, dims, u, b)
+    L = lf.LatticeFlow(kernel, "LatticeLevelReductions", dims)
+    L.setParam("pr_kernel", pr_kernel)
+    L.setParam("host_loops", host_loops)
+    L.setParam("tile_rows", tile_rows)
+    L.addEnergyPotentials(u, b)
+    L.run()
+    r = L.levels()
+    assert int(np.abs(r - r_ref).max()) <= R_TOL
+    assert int(r.sum()) == int(r_ref.sum())
+    sure = np.abs(r_ref) > R_TOL
+    assert np.array_equal(L.getCut()[sure], cut_ref[sure])
