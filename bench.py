@@ -57,8 +57,10 @@ def parse():
     ap.add_argument("--profile-run", action="store_true",
                     help="only warm-up and timed device-resident solves (for ncu captures)")
     ap.add_argument("--host-loops", action="store_true",
-                    help="one launch per pass instead of device-side pass loops (CUDA graphs with "
-                         "conditional nodes, whose kernels a profiler does not list); same kernels")
+                    help="one launch per pass (the default; kept for the recorded profiling commands)")
+    ap.add_argument("--device-loops", action="store_true",
+                    help="run the staged passes in device-side loops (CUDA graphs with conditional "
+                         "nodes, whose kernels a profiler does not list)")
     ap.add_argument("--tuning", default=None,
                     help="tile_rows,local_sweeps,launches_per_relabel instead of the autotuner "
                          "(e.g. the setting a bench run chose, for a profile run)")
@@ -261,8 +263,8 @@ def run_ours(args):
 
     tuning = None
     tune_table = None
-    if args.host_loops:
-        L.setParam("host_loops", 1)
+    if args.device_loops and not args.host_loops:
+        L.setParam("device_loops", 1)
     if args.tuning:
         tr_, sw_, lp_ = (int(x) for x in args.tuning.split(","))
         tuning = {"tile_rows": tr_, "local_sweeps": sw_, "launches_per_relabel": lp_}

@@ -154,7 +154,13 @@ int lf_set_tuning(lf_lattice* h, int tile_rows, int local_sweeps, int launches_p
  * negative = never), "tail_tree_nodes" (nodes of one such tree at most;
  * 0 = 65,536), "max_epochs" (global relabels per solve before the
  * solve gives up with LF_ERR_NO_CONVERGENCE; 0 = 1,000,000; the handle stays
- * usable).  LF_ERR_INVALID for an unknown name. */
+ * usable), "pr_kernel" (push/relabel pass of 2-d 3x3 lattices: 0 = staged by
+ * bulk tensor copies, 40 registers; 1 = generic tile kernel; 2 = staged, 32
+ * registers), "bfs_kernel" (global-relabel pass of those lattices: 0 =
+ * staged, 1 = generic), "device_loops" (1 = the staged passes of a relabel or
+ * an epoch run as one CUDA graph with a device-side loop; 0 = one launch per
+ * pass, the default).  Results never depend on these.  LF_ERR_INVALID for an
+ * unknown name. */
 int lf_set_param(lf_lattice* h, const char* name, int value);
 
 /* -------------------------------------------------------------- batches

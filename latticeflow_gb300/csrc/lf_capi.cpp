@@ -244,7 +244,7 @@ int lf_set_param(lf_lattice* h, const char* name, int value) {
     else if (n == "tail_tree_nodes") t.tail_tree_nodes = value;
     else if (n == "pr_kernel") t.pr_kernel = value;
     else if (n == "bfs_kernel") t.bfs_kernel = value;
-    else if (n == "host_loops") t.host_loops = value;
+    else if (n == "device_loops") t.device_loops = value;
     else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
   });
 }
@@ -557,7 +557,7 @@ int lf_batch_set_param(lf_batch* b, const char* name, int value) {
     else if (n == "tail_tree_nodes") t.tail_tree_nodes = value;
     else if (n == "pr_kernel") t.pr_kernel = value;
     else if (n == "bfs_kernel") t.bfs_kernel = value;
-    else if (n == "host_loops") t.host_loops = value;
+    else if (n == "device_loops") t.device_loops = value;
     else if (n == "defer_checks") b->b->defer_checks = value != 0;
     else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
   });

@@ -536,7 +536,7 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
   const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
   const long long cap = 4LL * tiles + 64;
   const int k2d = tune.bfs_kernel != 1 ? lattice2d_kernel_size(host[0], n == 1) : 0;
-  if (k2d && tune.host_loops != 1) {
+  if (k2d && tune.device_loops == 1) {
     // the whole relabel in one device-side loop: passes until no tile is
     // queued (a cap that ends it early is reported by activate())
     if (!loop_bfs) loop_bfs = pass_loop_new();
@@ -556,7 +556,7 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
     if (!pool_maps) pool_maps = pool_maps_new();
     maps = pool_maps_bfs(pool_maps, host, h, mask, stream);
   }
-  if (maps && tune.host_loops != 1) {
+  if (maps && tune.device_loops == 1) {
     if (!loop_bfs) loop_bfs = pass_loop_new();
     PoolBFS p{host[0], d_inst, d_tile_inst, h, mask, q, 0, 64, d_flag, d_counters};
     mark(1, false);
@@ -700,7 +700,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
       if (k64) {
         if (!loop_pr) loop_pr = pass_loop_new();
         mark(0, false);
-        if (tune.host_loops != 1) {
+        if (tune.device_loops == 1) {
           check(pr2d64(loop_pr, p, k64, d_counters + 4, std::max(tiles, 1), d_ctl, (unsigned)M,
                        d_counters + 6, stream),
                 "push-relabel loop (TMA, 64-bit)");
@@ -732,7 +732,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
         if (!pool_maps) pool_maps = pool_maps_new();
         pmaps = pool_maps_pr(pool_maps, host, res, exc, h, stream);
       }
-      if (pmaps && tune.host_loops != 1) {
+      if (pmaps && tune.device_loops == 1) {
         if (!loop_pr) loop_pr = pass_loop_new();
         mark(0, false);
         check(pool_pr2d(loop_pr, pmaps, p, tb_pool, pr2d_variant(tune.pr_kernel), d_counters + 4,
@@ -743,7 +743,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
         drain_queue();
         continue;
       }
-      if (k2d && tune.host_loops != 1) {
+      if (k2d && tune.device_loops == 1) {
         // M passes (fewer when the queue runs dry) in one device-side loop
         if (!loop_pr) loop_pr = pass_loop_new();
         mark(0, false);
@@ -793,6 +793,7 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
   stats.bfs_passes += (long long)c[5];
   stats.pr_launches += (long long)c[6];
   if (hooks) hooks->launches += 2 * (long long)(c[5] + c[6]);  // pass + control kernel per pass
+  if (c[4] == 2) throw LfError{6, "a queued tile id was out of range"};
   if (c[4]) throw LfError{6, "a tile's staging copy did not complete in time"};
   if (c[7]) throw LfError{4, "global relabel did not converge"};
 }

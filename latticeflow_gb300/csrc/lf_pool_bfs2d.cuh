@@ -44,6 +44,10 @@ template <int TB>
 __device__ __forceinline__ void bfs2d_issue(const BFS2dMaps& maps, const Geo& g, int tile,
                                             unsigned stage, unsigned bar) {
   using Ly = BFS2dLayout<TB>;
+  if (!tile_ok(tile, g.ntiles)) {
+    mbar_expect_tx(bar, 0);
+    return;
+  }
   const int tc = tile % g.ntc, tb = tile / g.ntc;
   const int b0 = tb * TB, c0 = tc * 32;
   mbar_expect_tx(bar, Ly::tx_bytes);
@@ -183,6 +187,11 @@ __global__ void __launch_bounds__(TB * 32, 2048 / (TB * 32))
       mbar_wait_bounded(bar, par, kPr2dWaitLimit);
       if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
       return;
+    }
+    if (!tile_ok(gt, g.ntiles)) {
+      if (threadIdx.x == 0) atomicExch(fault, 2ull);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      continue;
     }
     bfs2d_tile<K, TB>(p, g, cur, st, s_flags + buf, gt, h0, m);
   }

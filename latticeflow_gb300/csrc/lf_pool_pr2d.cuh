@@ -171,10 +171,22 @@ __device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap* map
 
 constexpr int kPr2dWaitLimit = 1 << 20;  // try_wait rounds before a copy counts as lost
 
+// A tile id taken from a queue must name a tile of the lattice; one that does
+// not is recorded (fault flag 2) and skipped: its copies are not issued (the
+// stage barrier's phase is completed by an arrival without bytes) and it is
+// not visited.
+__device__ __forceinline__ bool tile_ok(int gt, int ntiles) {
+  return (unsigned)gt < (unsigned)ntiles;
+}
+
 template <int K, int TB>
 __device__ __forceinline__ void pr2d_issue(const PR2dMaps& maps, const Geo& g, int tile,
                                            unsigned stage, unsigned bar) {
   using Ly = PR2dLayout<K, TB>;
+  if (!tile_ok(tile, g.ntiles)) {
+    mbar_expect_tx(bar, 0);
+    return;
+  }
   const int tc = tile % g.ntc, tb = tile / g.ntc;
   const int b0 = tb * TB, c0 = tc * 32;
   mbar_expect_tx(bar, Ly::tx_bytes);
@@ -360,6 +372,11 @@ __global__ void __maxnreg__(REGS)
       if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
       return;
     }
+    if (!tile_ok(gt, g.ntiles)) {
+      if (threadIdx.x == 0) atomicExch(fault, 2ull);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      continue;
+    }
     pr2d_tile<K, TB>(p, g, hmax, cur, reinterpret_cast<int*>(st),
                             reinterpret_cast<int*>(st + Ly::res_bytes),
                             reinterpret_cast<int*>(st + Ly::res_bytes + Ly::exc_bytes), gt, e0, h0);
@@ -394,6 +411,10 @@ template <int K, int TB>
 __device__ __forceinline__ void pr2d64_issue(const PR2dMaps64& maps, const Geo& g, int tile,
                                              unsigned stage, unsigned bar) {
   using Ly = PR2dLayout64<K, TB>;
+  if (!tile_ok(tile, g.ntiles)) {
+    mbar_expect_tx(bar, 0);
+    return;
+  }
   const int tc = tile % g.ntc, tb = tile / g.ntc;
   const int b0 = tb * TB, c0 = tc * 32;
   mbar_expect_tx(bar, Ly::tx_bytes);
@@ -458,6 +479,11 @@ __global__ void __launch_bounds__(TB * 32)
       mbar_wait_bounded(bar, par, kPr2dWaitLimit);
       if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
       return;
+    }
+    if (!tile_ok(gt, g.ntiles)) {
+      if (threadIdx.x == 0) atomicExch(fault, 2ull);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      continue;
     }
     pr2d_tile<K, TB, Geo, long long>(p, g, hmax, cur, s_res, s_exc, s_h, gt, e0, h0, s_km);
   }

@@ -29,8 +29,9 @@ struct Tuning {
                                  // with 32 registers
   int bfs_kernel = 0;            // BFS pass of a single 2-d lattice: 0 = TMA-staged,
                                  // 1 = generic tile kernel
-  int host_loops = 0;            // TMA-staged passes: 0 = device-side pass loops (CUDA
-                                 // graphs), 1 = one launch per pass from the host
+  int device_loops = 0;          // TMA-staged passes: 1 = device-side pass loops (CUDA
+                                 // graphs with conditional nodes), 0 = one launch per
+                                 // pass from the host
 };
 
 struct SolveStats {

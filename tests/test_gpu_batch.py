@@ -90,9 +90,9 @@ def test_batch_3d_and_errors(native, gpu, oracle_port):
         B2.add("Star2d_16", (8, 8))    # at most two kernel sizes
 
 
-@pytest.mark.parametrize("pr_kernel,bfs_kernel,host_loops", [(0, 0, 0), (0, 0, 1), (1, 1, 1), (2, 0, 0)])
+@pytest.mark.parametrize("pr_kernel,bfs_kernel,device_loops", [(0, 0, 1), (0, 0, 0), (1, 1, 0), (2, 0, 1)])
 @pytest.mark.parametrize("tile_rows", [8, 16, 32])
-def test_batch_pass_variants(native, gpu, oracle_port, pr_kernel, bfs_kernel, host_loops, tile_rows):
+def test_batch_pass_variants(native, gpu, oracle_port, pr_kernel, bfs_kernel, device_loops, tile_rows):
     """A pool of mixed 4- and 8-connected lattices through the TMA-staged pool
     passes (device-side loops or one launch per pass) and the generic tile
     passes: every lattice gets the oracle's energy and both cut sets."""
@@ -105,7 +105,7 @@ def test_batch_pass_variants(native, gpu, oracle_port, pr_kernel, bfs_kernel, ho
         B.add(p.kernel, p.dims)
     B.setParam("pr_kernel", pr_kernel)
     B.setParam("bfs_kernel", bfs_kernel)
-    B.setParam("host_loops", host_loops)
+    B.setParam("device_loops", device_loops)
     B.setParam("tile_rows", tile_rows)
     B.setParam("local_sweeps", 2)
     B.setParam("launches_per_relabel", 4)

@@ -224,15 +224,15 @@ def test_pinned_host_arrays_read_in_place(native, gpu):
     assert d.flow() == e.flow() and np.array_equal(d.getCut(), e.getCut())
 
 
-@pytest.mark.parametrize("pr_kernel,bfs_kernel,host_loops", [(0, 0, 0), (0, 0, 1), (1, 1, 0), (2, 0, 0),
-                                                              (1, 0, 0), (0, 1, 0)])
+@pytest.mark.parametrize("pr_kernel,bfs_kernel,device_loops", [(0, 0, 1), (0, 0, 0), (1, 1, 1), (2, 0, 1),
+                                                                (1, 0, 1), (0, 1, 1)])
 @pytest.mark.parametrize("kernel,dims,tile_rows", [
     ("Full2d_8", (200, 230), 8), ("Full2d_8", (256, 160), 16), ("Full2d_8", (97, 300), 32),
     ("Full2d_4", (210, 190), 16), ("Full2d_4", (64, 500), 32)], ids=lambda v: str(v))
-def test_push_relabel_kernels_agree(native, gpu, oracle_port, pr_kernel, bfs_kernel, host_loops,
+def test_push_relabel_kernels_agree(native, gpu, oracle_port, pr_kernel, bfs_kernel, device_loops,
                                     kernel, dims, tile_rows):
     """The TMA-staged 2-d passes (pr_kernel 0, 2; bfs_kernel 0), in
-    device-side loops (host_loops 0) or launched one by one (1), and the
+    device-side loops (device_loops 1) or launched one by one (0), and the
     generic tile passes (1) give the reference's exact answer at every tile
     height."""
     import latticeflow_gb300 as lf
@@ -243,7 +243,7 @@ def test_push_relabel_kernels_agree(native, gpu, oracle_port, pr_kernel, bfs_ker
     L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
     L.setParam("pr_kernel", pr_kernel)
     L.setParam("bfs_kernel", bfs_kernel)
-    L.setParam("host_loops", host_loops)
+    L.setParam("device_loops", device_loops)
     L.setTuning(tile_rows=tile_rows, local_sweeps=3, launches_per_relabel=4)
     L.addEnergyPotentials(u, b)
     L.run()
@@ -277,12 +277,12 @@ def test_tma_pass_full_size_all_variants(native, gpu, oracle_port):
     p = W.large_cut(0)
     u, b = p.energies()
     ref = None
-    for prk, rows, hl in ((1, 16, 1), (0, 16, 0), (0, 16, 1), (2, 16, 0), (0, 8, 0), (2, 8, 0),
-                          (0, 32, 0), (2, 32, 0)):
+    for prk, rows, dl in ((1, 16, 0), (0, 16, 1), (0, 16, 0), (2, 16, 1), (0, 8, 1), (2, 8, 0),
+                          (0, 32, 1), (2, 32, 0)):
         L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
         L.setParam("pr_kernel", prk)
         L.setParam("bfs_kernel", 1 if ref is None else 0)  # the reference run: generic passes
-        L.setParam("host_loops", hl)
+        L.setParam("device_loops", dl)
         L.setTuning(tile_rows=rows, local_sweeps=2, launches_per_relabel=8)
         for _ in range(2):
             L.clear()

@@ -90,12 +90,12 @@ def test_level_reductions_vs_oracle(native, gpu, oracle_port, kernel, dims):
 
 
 @pytest.mark.parametrize("kernel,dims", [("Full2d_4", (70, 66)), ("Full2d_8", (45, 52))])
-@pytest.mark.parametrize("pr_kernel,host_loops,tile_rows", [(0, 0, 8), (0, 0, 16), (0, 1, 32),
-                                                            (1, 0, 16), (1, 1, 32)])
+@pytest.mark.parametrize("pr_kernel,device_loops,tile_rows", [(0, 1, 8), (0, 1, 16), (0, 0, 32),
+                                                              (1, 1, 16), (1, 0, 32)])
 def test_level_reductions_pass_variants(native, gpu, oracle_port, kernel, dims, pr_kernel,
-                                        host_loops, tile_rows):
+                                        device_loops, tile_rows):
     """Section solves through the TMA-staged 64-bit pass with section masks
-    (pr_kernel 0; device-side loops or one launch per pass) and the generic
+    (pr_kernel 0; one launch per pass or device-side loops) and the generic
     tile pass (1): levels within one raw unit of the oracle, totals exact."""
     import latticeflow_gb300 as lf
     O = oracle_port
@@ -110,7 +110,7 @@ def test_level_reductions_pass_variants(native, gpu, oracle_port, kernel, dims, 
     r_ref, cut_ref, _ = O.port_pf(kernel, dims, u, b)
     L = lf.LatticeFlow(kernel, "LatticeLevelReductions", dims)
     L.setParam("pr_kernel", pr_kernel)
-    L.setParam("host_loops", host_loops)
+    L.setParam("device_loops", device_loops)
     L.setParam("tile_rows", tile_rows)
     L.addEnergyPotentials(u, b)
     L.run()
