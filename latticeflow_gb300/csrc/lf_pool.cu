@@ -533,7 +533,7 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
   check(cudaGetLastError(), "bfs setup");
   const size_t smem = sizeof(PoolSmemHead) + size_t(hv_max) * sizeof(int);
   const int grid = std::max(tiles, 1);
-  const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
+  const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 6;
   const long long cap = 4LL * tiles + 64;
   const int k2d = tune.bfs_kernel != 1 ? lattice2d_kernel_size(host[0], n == 1) : 0;
   if (k2d && tune.device_loops == 1) {
@@ -810,7 +810,7 @@ void PoolRunner::reach(const T* exc, const uint64_t* mask, int* markv, SolveStat
   int NTmax = threads;
   const size_t smem = sizeof(PoolSmemHead) + size_t(NTmax) * sizeof(int);
   const int grid = std::max(tiles, 1);
-  const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 4;
+  const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 6;
   const long long cap = 4LL * tiles + 64;
   int cur = 0;
   for (long long pass = 0;;) {
