@@ -111,8 +111,9 @@ struct PR2dLayout {
   static constexpr int h_bytes = HR * kPr2dHaloW * 4;
   static constexpr int stage_bytes = (res_bytes + exc_bytes + h_bytes + 127) / 128 * 128;
   static constexpr int tx_bytes = res_bytes + exc_bytes + h_bytes;
-  // two stage buffers, two mbarriers, alignment slack
-  static constexpr int smem_bytes = 2 * stage_bytes + 16 + 128;
+  // two stage buffers, two mbarriers, a neighbour-tile flag word per buffer,
+  // alignment slack
+  static constexpr int smem_bytes = 2 * stage_bytes + 32 + 128;
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -179,6 +180,17 @@ __device__ __forceinline__ bool tile_ok(int gt, int ntiles) {
   return (unsigned)gt < (unsigned)ntiles;
 }
 
+// Neighbour-tile flag of a tile offset (dtb, dtc) in {-1, 0, 1}^2, not both
+// 0: bit 0 up, 1 down, 2 left, 3 right, 4 up-left, 5 up-right, 6 down-left,
+// 7 down-right (the layout of bfs2d_edge_bits).
+__device__ __forceinline__ unsigned nbr_bit(int dtb, int dtc) {
+  const int code = (dtb + 1) * 3 + (dtc + 1);  // 0..8, 4 = the tile itself
+  // code: 0 (-1,-1) 1 (-1,0) 2 (-1,1) 3 (0,-1) 5 (0,1) 6 (1,-1) 7 (1,0) 8 (1,1)
+  constexpr unsigned kBit = (4u << 0) | (0u << 3) | (5u << 6) | (2u << 9) | (0u << 12) |
+                            (3u << 15) | (6u << 18) | (1u << 21) | (7u << 24);
+  return code == 4 ? 0u : 1u << ((kBit >> (3 * code)) & 7u);
+}
+
 template <int K, int TB>
 __device__ __forceinline__ void pr2d_issue(const PR2dMaps& maps, const Geo& g, int tile,
                                            unsigned stage, unsigned bar) {
@@ -207,10 +219,15 @@ __device__ __forceinline__ void pr2d_issue(const PR2dMaps& maps, const Geo& g, i
 // T: capacity type (int for binary cuts, long long for parametric / TV
 // section solves); km: the node's staged section mask (bit k: direction k
 // stays inside the node's section), or null when the pass has none.
+//
+// s_nbr: the visit's neighbour-tile flags (bit layout of bfs2d_edge_bits),
+// zero at entry.  A push across the tile edge only sets the bit of the tile
+// it reached; each flagged tile is queued once after the visit's last
+// barrier, so no pushing thread waits on a global queue atomic.
 template <int K, int TB, class LAT, class T = int>
 __device__ __forceinline__ void pr2d_tile(const PoolPR<T>& p, const LAT& L, int hmax, int cur,
                                           T* s_res, T* s_exc, int* s_h, int tile,
-                                          const T e0, int my_h,
+                                          const T e0, int my_h, unsigned* s_nbr,
                                           const uint64_t* s_km = nullptr) {
   constexpr int NT = TB * 32;
   constexpr int HW = kPr2dHaloW;
@@ -231,6 +248,7 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<T>& p, const LAT& L, int 
     const int nb = ib + s2_db<K>(k), nc = ic + s2_dc<K>(k);
     if (nb < 0 || nb >= TB || nc < 0 || nc >= 32) outm |= 1u << k;
   }
+  unsigned nbr = 0;  // neighbour tiles this thread's pushes reached
   for (int it = 0; it < p.sweeps; ++it) {
     T e = s_exc[t];
     // a node parked at the epoch cap no longer relabels but still pushes
@@ -265,7 +283,7 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<T>& p, const LAT& L, int 
           // neighbour leaves this tile's rows / columns
           const int dtb = (s2_db<K>(k) < 0 && ib == 0) ? -1 : (s2_db<K>(k) > 0 && ib == TB - 1) ? 1 : 0;
           const int dtc = (s2_dc<K>(k) < 0 && ic == 0) ? -1 : (s2_dc<K>(k) > 0 && ic == 31) ? 1 : 0;
-          enqueue_tile(p.q, nxt, tile_g + dtb * lat_ntc(L) + dtc);
+          nbr |= nbr_bit(dtb, dtc);
         }
       }
       if (sent) atom_add(&s_exc[t], (T)-sent);
@@ -301,11 +319,23 @@ __device__ __forceinline__ void pr2d_tile(const PoolPR<T>& p, const LAT& L, int 
   for (int k = 0; k < K; ++k)  // edges across the tile edge were updated by their pushes
     if (!((outm >> k) & 1u)) res[(long long)k * lat_plane(L) + gi] = s_res[k * NT + t];
   p.h[gi] = my_h;
+  nbr = __reduce_or_sync(0xffffffffu, nbr);
+  if (ic == 0 && nbr) atomicOr(s_nbr, nbr);
   // the buffer's next contents come from the async proxy: order this
   // visit's shared-memory accesses before them
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   const int still = ef > 0 && my_h < hmax;
-  if (__syncthreads_or(still) && t == 0) enqueue_tile(p.q, nxt, tile_g);
+  const bool again = __syncthreads_or(still);
+  if (t < 8) {
+    const unsigned f = *s_nbr;
+    if ((f >> t) & 1u) {
+      const int dtb = (t == 0 || t == 4 || t == 5) ? -1 : (t == 1 || t == 6 || t == 7) ? 1 : 0;
+      const int dtc = (t == 2 || t == 4 || t == 6) ? -1 : (t == 3 || t == 5 || t == 7) ? 1 : 0;
+      // a bit is set only by a push, which never leaves the lattice
+      enqueue_tile(p.q, nxt, tile_g + dtb * lat_ntc(L) + dtc);
+    }
+  }
+  if (again && t == 0) enqueue_tile(p.q, nxt, tile_g);
 }
 
 // One lattice (the pool of one), no section mask, 32-bit capacities.
@@ -325,6 +355,9 @@ __global__ void __maxnreg__(REGS)
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<unsigned long long>(smem_raw) + 127) & ~127ull);
   const unsigned bar0 = smem_addr(smem + 2 * Ly::stage_bytes);  // two mbarriers, 8 bytes apart
+  // neighbour-tile flags of the visit on each buffer: a word is cleared two
+  // visits after its last readers, who have passed two barriers since
+  unsigned* s_nbr = reinterpret_cast<unsigned*>(smem + 2 * Ly::stage_bytes + 16);
   const unsigned stage0 = smem_addr(smem);
   const Geo& g = p.inst0.g;
   const int cur = ctl ? *ctl : p.cur;
@@ -347,6 +380,7 @@ __global__ void __maxnreg__(REGS)
     if (threadIdx.x == 0) {
       p.q.flag[cur][gt] = 0;
       atomicAdd(&p.counters[0], 1ull);
+      s_nbr[buf] = 0;
     }
     if (done) continue;
     // the next tile of this CTA: its copies fly while this one is worked on
@@ -379,7 +413,8 @@ __global__ void __maxnreg__(REGS)
     }
     pr2d_tile<K, TB>(p, g, hmax, cur, reinterpret_cast<int*>(st),
                             reinterpret_cast<int*>(st + Ly::res_bytes),
-                            reinterpret_cast<int*>(st + Ly::res_bytes + Ly::exc_bytes), gt, e0, h0);
+                            reinterpret_cast<int*>(st + Ly::res_bytes + Ly::exc_bytes), gt, e0, h0,
+                            s_nbr + buf);
   }
 }
 
@@ -404,7 +439,7 @@ struct PR2dLayout64 {
   static constexpr int km_off = (h_off + h_bytes + 127) / 128 * 128;
   static constexpr int stage_bytes = km_off + NT * 8;
   static constexpr int tx_bytes = res_bytes + NT * 8 + h_bytes + NT * 8;
-  static constexpr int smem_bytes = 2 * stage_bytes + 16 + 128;
+  static constexpr int smem_bytes = 2 * stage_bytes + 32 + 128;
 };
 
 template <int K, int TB>
@@ -435,6 +470,7 @@ __global__ void __launch_bounds__(TB * 32)
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<unsigned long long>(smem_raw) + 127) & ~127ull);
   const unsigned bar0 = smem_addr(smem + 2 * Ly::stage_bytes);
+  unsigned* s_nbr = reinterpret_cast<unsigned*>(smem + 2 * Ly::stage_bytes + 16);
   const unsigned stage0 = smem_addr(smem);
   const Geo& g = p.inst0.g;
   const int cur = ctl ? *ctl : p.cur;
@@ -457,6 +493,7 @@ __global__ void __launch_bounds__(TB * 32)
     if (threadIdx.x == 0) {
       p.q.flag[cur][gt] = 0;
       atomicAdd(&p.counters[0], 1ull);
+      s_nbr[buf] = 0;
     }
     if (done) continue;
     const unsigned nx = i + gridDim.x;
@@ -485,7 +522,8 @@ __global__ void __launch_bounds__(TB * 32)
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       continue;
     }
-    pr2d_tile<K, TB, Geo, long long>(p, g, hmax, cur, s_res, s_exc, s_h, gt, e0, h0, s_km);
+    pr2d_tile<K, TB, Geo, long long>(p, g, hmax, cur, s_res, s_exc, s_h, gt, e0, h0, s_nbr + buf,
+                                     s_km);
   }
 }
 
@@ -501,7 +539,7 @@ struct PR2dPoolLayout {
   static constexpr int h_off = exc_off + NT * 4;
   static constexpr int h_bytes = (TB + 2) * kPr2dHaloW * 4;
   static constexpr int stage_bytes = (h_off + h_bytes + 127) / 128 * 128;
-  static constexpr int smem_bytes = 2 * stage_bytes + 16 + 128;
+  static constexpr int smem_bytes = 2 * stage_bytes + 32 + 128;
 };
 
 // A lattice's three tensor maps (residual planes, excess, heights) in the
@@ -536,6 +574,7 @@ __global__ void __maxnreg__(REGS)
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<unsigned long long>(smem_raw) + 127) & ~127ull);
   const unsigned bar0 = smem_addr(smem + 2 * Ly::stage_bytes);
+  unsigned* s_nbr = reinterpret_cast<unsigned*>(smem + 2 * Ly::stage_bytes + 16);
   const unsigned stage0 = smem_addr(smem);
   const int cur = ctl ? *ctl : p.cur;
   const unsigned n = queued_count(p.q, cur);
@@ -555,6 +594,7 @@ __global__ void __maxnreg__(REGS)
     if (threadIdx.x == 0) {
       p.q.flag[cur][gt] = 0;
       atomicAdd(&p.counters[0], 1ull);
+      s_nbr[buf] = 0;
     }
     const unsigned nx = i + gridDim.x;
     if (threadIdx.x == 0 && nx < n)
@@ -585,9 +625,9 @@ __global__ void __maxnreg__(REGS)
     const Lat2d L = lat2d_of(I);
     const int tile = gt - L.tile_base;
     if (I.st.K == 8)
-      pr2d_tile<8, TB>(p, L, I.hmax, cur, s_res, s_exc, s_h, tile, e0, h0);
+      pr2d_tile<8, TB>(p, L, I.hmax, cur, s_res, s_exc, s_h, tile, e0, h0, s_nbr + buf);
     else
-      pr2d_tile<4, TB>(p, L, I.hmax, cur, s_res, s_exc, s_h, tile, e0, h0);
+      pr2d_tile<4, TB>(p, L, I.hmax, cur, s_res, s_exc, s_h, tile, e0, h0, s_nbr + buf);
   }
 }
 
