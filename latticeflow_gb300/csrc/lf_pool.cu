@@ -12,7 +12,10 @@
 //   }
 // Node pools hold all lattices back to back (node_base), residual planes
 // likewise (res_base); the persistent kernels take whatever tile is queued
-// next, from any lattice.
+// next, from any lattice.  Passes: the TMA-staged 2-d kernels
+// (lf_pool_pr2d.cuh, lf_pool_bfs2d.cuh) for lattices with 3x3
+// neighbourhoods, the generic tile kernels otherwise; one launch per pass,
+// or (device_loops) the passes of a relabel / an epoch in one CUDA graph.
 #include <algorithm>
 #include <chrono>
 #include <climits>
@@ -694,7 +697,8 @@ void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t*
     }
     if constexpr (std::is_same<T, long long>::value) {
       // 64-bit capacities with section masks on one 2-d lattice (parametric /
-      // TV section solves): the TMA-staged pass, in a device-side loop
+      // TV section solves): the TMA-staged pass, one launch per pass (or a
+      // device-side loop of passes when device_loops is set)
       PoolPR<long long> p{host[0], d_inst, d_tile_inst, res, exc, h, kmask, q, 0, R, d_counters};
       const int k64 = tune.pr_kernel != 1 ? pr2d64_kernel_size(p, n == 1) : 0;
       if (k64) {
