@@ -73,10 +73,10 @@ __device__ void pr_tile(const PoolPR<T>& p, const InstDesc& I, PoolSmemHead* hd,
     hd->hoff[t] = (st.da[t] * x.HBB + st.db[t]) * x.HCC + st.dc[t];
     hd->toff[t] = (st.da[t] * g.TB + st.db[t]) * g.TC + st.dc[t];
   }
-  if (t == 0) hd->nbr = 0;  // its readers of the last visit passed the loop's barrier
-  // neighbour tiles this thread's pushes reached: bit (da+1)*9 + (db+1)*3 +
-  // (dc+1) of the tile offset (every stencil's halo fits in one tile)
-  unsigned nbr = 0;
+  // neighbour tiles reached by this visit's pushes: bit (da+1)*9 + (db+1)*3 +
+  // (dc+1) of the tile offset (every stencil's halo fits in one tile); its
+  // readers of the last visit have passed the loop's barrier
+  if (t == 0) hd->nbr = 0;
   load_halo_heights(g, st, x, h, s_h);
   uint64_t outm = 0;
   T e0 = 0;
@@ -127,7 +127,7 @@ __device__ void pr_tile(const PoolPR<T>& p, const InstDesc& I, PoolSmemHead* hd,
           const int dta = A_ < x.a0 ? -1 : A_ >= x.a0 + g.TA ? 1 : 0;
           const int dtb = B_ < x.b0 ? -1 : B_ >= x.b0 + g.TB ? 1 : 0;
           const int dtc = C_ < x.c0 ? -1 : C_ >= x.c0 + g.TC ? 1 : 0;
-          nbr |= 1u << ((dta + 1) * 9 + (dtb + 1) * 3 + (dtc + 1));
+          atomicOr(&hd->nbr, 1u << ((dta + 1) * 9 + (dtb + 1) * 3 + (dtc + 1)));
         }
       }
       if (sent) atom_add(&s_exc[t], (T)-sent);
@@ -167,8 +167,6 @@ __device__ void pr_tile(const PoolPR<T>& p, const InstDesc& I, PoolSmemHead* hd,
     h[x.gi] = my_h;
     still = ef > 0 && my_h < hmax;
   }
-  nbr = __reduce_or_sync(0xffffffffu, nbr);
-  if ((t & 31) == 0 && nbr) atomicOr(&hd->nbr, nbr);
   const bool again = __syncthreads_or(still);
   // each neighbour tile reached is queued once (27 threads, bit 13 = this tile)
   if (t < 27 && t != 13 && ((hd->nbr >> t) & 1u)) {
