@@ -202,7 +202,8 @@ void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device
   // transfer overlaps the fill instead of preceding it
   const int64_t* mu = device_ptrs ? nullptr : (const int64_t*)mapped_host_ptr(unary);
   const int64_t* mb = device_ptrs ? nullptr : (const int64_t*)mapped_host_ptr(binary);
-  if (mu && mb) {
+  const bool in_place = mu && mb;  // read over the host link: each table once (scatter)
+  if (in_place) {
     du = mu;
     db = mb;
     device_ptrs = true;
@@ -219,7 +220,8 @@ void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device
     check(counted(launch_fill_energy_pf(g, st, nd, N, du, db, d_exc64, d_cap64, d_err, stream)),
           "fill energy");
   else
-    check(counted(launch_fill_energy(g, st, nd, N, du, db, d_exc64, d_cap64, d_c0, d_err, stream)),
+    check(counted(launch_fill_energy(g, st, nd, N, du, db, d_exc64, d_cap64, d_c0, d_err, !in_place,
+                                          stream)),
           "fill energy");
   if (tu) cudaFreeAsync(tu, stream);
   if (tb) cudaFreeAsync(tb, stream);
