@@ -159,7 +159,10 @@ int lf_set_tuning(lf_lattice* h, int tile_rows, int local_sweeps, int launches_p
  * registers), "bfs_kernel" (global-relabel pass of those lattices: 0 =
  * staged, 1 = generic), "device_loops" (1 = the staged passes of a relabel or
  * an epoch run as one CUDA graph with a device-side loop; 0 = one launch per
- * pass, the default).  Results never depend on these.  LF_ERR_INVALID for an
+ * pass, the default), "fill_kernel" (energy fill of device-resident arrays:
+ * 0 = gathered with one lane per filling edge, 1 = gathered per node, 2 =
+ * scattered with atomics, the form always used for pinned host arrays read
+ * in place).  Results never depend on these.  LF_ERR_INVALID for an
  * unknown name. */
 int lf_set_param(lf_lattice* h, const char* name, int value);
 

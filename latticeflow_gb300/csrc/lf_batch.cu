@@ -150,7 +150,7 @@ void Batch::add_energy(int i, const int64_t* unary, const int64_t* binary) {
   check(cudaMemcpyAsync(buf, unary, ub, cudaMemcpyHostToDevice, stream), "memcpy");
   check(cudaMemcpyAsync(buf + 2 * m.N, binary, bb, cudaMemcpyHostToDevice, stream), "memcpy");
   check(launch_fill_energy(m.g, m.st, m.nd, m.N, buf, buf + 2 * m.N, d_exc64 + m.node_base,
-                           d_cap64 + m.res_base, d_c0 + i, d_err, true, stream), "fill energy");
+                           d_cap64 + m.res_base, d_c0 + i, d_err, tune.fill_kernel, stream), "fill energy");
   cudaFreeAsync(buf, stream);
   solved = false;
   if (!defer_checks) check_err("pairwise term is not submodular (E00 + E11 > E01 + E10)");

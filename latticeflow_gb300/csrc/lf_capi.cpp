@@ -245,6 +245,7 @@ int lf_set_param(lf_lattice* h, const char* name, int value) {
     else if (n == "pr_kernel") t.pr_kernel = value;
     else if (n == "bfs_kernel") t.bfs_kernel = value;
     else if (n == "device_loops") t.device_loops = value;
+    else if (n == "fill_kernel") t.fill_kernel = value;
     else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
   });
 }
@@ -558,6 +559,7 @@ int lf_batch_set_param(lf_batch* b, const char* name, int value) {
     else if (n == "pr_kernel") t.pr_kernel = value;
     else if (n == "bfs_kernel") t.bfs_kernel = value;
     else if (n == "device_loops") t.device_loops = value;
+    else if (n == "fill_kernel") t.fill_kernel = value;
     else if (n == "defer_checks") b->b->defer_checks = value != 0;
     else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
   });

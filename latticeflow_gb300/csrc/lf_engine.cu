@@ -220,7 +220,8 @@ void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device
     check(counted(launch_fill_energy_pf(g, st, nd, N, du, db, d_exc64, d_cap64, d_err, stream)),
           "fill energy");
   else
-    check(counted(launch_fill_energy(g, st, nd, N, du, db, d_exc64, d_cap64, d_c0, d_err, !in_place,
+    check(counted(launch_fill_energy(g, st, nd, N, du, db, d_exc64, d_cap64, d_c0, d_err,
+                                          in_place ? 2 : tune.fill_kernel,
                                           stream)),
           "fill energy");
   if (tu) cudaFreeAsync(tu, stream);

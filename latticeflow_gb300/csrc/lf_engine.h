@@ -16,7 +16,7 @@ namespace lfg {
 // per-lattice element kernels (lf_kernels.cu)
 cudaError_t launch_fill_energy(const Geo& g, const Stencil& st, int nd, long long N,
                                const int64_t* u, const int64_t* b, long long* exc, long long* cap,
-                               long long* c0, int* err, bool gather, cudaStream_t s);
+                               long long* c0, int* err, int form, cudaStream_t s);
 cudaError_t launch_fill_energy_pf(const Geo& g, const Stencil& st, int nd, long long N,
                                   const int64_t* u, const int64_t* b, long long* exc,
                                   long long* cap, int* err, cudaStream_t s);

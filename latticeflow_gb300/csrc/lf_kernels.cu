@@ -97,24 +97,25 @@ __global__ void k_fill_energy(Geo g, Stencil st, int nd, long long N, const int6
 // pairwise terms (w -> w + d_e) and the target-side share of the terms that
 // end at it (the table of node w - d_e, edge e).  Every output word has one
 // writer, so the accumulation is a plain read-modify-write, and the integer
-// sums equal the scattered ones exactly.  Returns the node's share of the
-// constant term; *bad is set for a non-submodular own term.
+// sums equal the scattered ones exactly.
 template <bool VEC>
-__host__ __device__ __forceinline__ long long fill_gather_node(
-    const Geo& g, const Stencil& st, long long r, int a, int b, int c, const int64_t* unary,
-    const int64_t* binary, long long* exc, long long* cap, bool* bad) {
-  const int Kp = st.K / 2;
-  const long long w = ((long long)a * g.Bp + b) * g.Cp + c;
-  auto table = [&](long long node, int e, long long& A, long long& B, long long& C, long long& D) {
-    const int64_t* q = binary + (node * Kp + e) * 4;
-    if (VEC) {
-      const longlong2 q0 = reinterpret_cast<const longlong2*>(q)[0];
-      const longlong2 q1 = reinterpret_cast<const longlong2*>(q)[1];
-      A = q0.x; B = q0.y; C = q1.x; D = q1.y;
-    } else {
-      A = q[0]; B = q[1]; C = q[2]; D = q[3];
-    }
-  };
+__host__ __device__ __forceinline__ void fill_table(const int64_t* binary, int Kp, long long node,
+                                                    int e, long long& A, long long& B,
+                                                    long long& C, long long& D) {
+  const int64_t* q = binary + (node * Kp + e) * 4;
+  if (VEC) {
+    const longlong2 q0 = reinterpret_cast<const longlong2*>(q)[0];
+    const longlong2 q1 = reinterpret_cast<const longlong2*>(q)[1];
+    A = q0.x; B = q0.y; C = q1.x; D = q1.y;
+  } else {
+    A = q[0]; B = q[1]; C = q[2]; D = q[3];
+  }
+}
+
+// Unary share of node r: returns E0 - E1 and adds E0 to *c0.
+template <bool VEC>
+__host__ __device__ __forceinline__ long long fill_gather_unary(const int64_t* unary, long long r,
+                                                               long long* c0) {
   long long E0, E1;
   if (VEC) {
     const longlong2 ue = reinterpret_cast<const longlong2*>(unary)[r];
@@ -124,55 +125,69 @@ __host__ __device__ __forceinline__ long long fill_gather_node(
     E0 = unary[2 * r];
     E1 = unary[2 * r + 1];
   }
-  long long x = E0 - E1, c0 = E0;
-  for (int e = 0; e < Kp; ++e) {
-    const int da = st.da[e], db = st.db[e], dc = st.dc[e];
-    long long A, B, C, D;
-    if (a + da >= 0 && a + da < g.A && b + db >= 0 && b + db < g.B && c + dc >= 0 &&
-        c + dc < g.C) {  // own term, w is its source end
-      table(r, e, A, B, C, D);
-      c0 += A;
-      const long long Bq = B - A, Cq = C - D;
-      if (Bq + Cq < 0) *bad = true;
-      long long cu = 0;
-      x += A - D;
-      if (Bq < 0) { x += Bq; cu = Bq + Cq; }
-      else if (Cq < 0) x -= Cq;
-      else cu = Cq;
-      if (cu) cap[(long long)e * g.NP + w] += cu;
-    }
-    const int sa = a - da, sb = b - db, sc = c - dc;
-    if (sa >= 0 && sa < g.A && sb >= 0 && sb < g.B && sc >= 0 && sc < g.C) {  // w is the target
-      table(((long long)sa * g.B + sb) * g.C + sc, e, A, B, C, D);
-      const long long Bq = B - A, Cq = C - D;
-      long long cv = 0;
-      if (Bq < 0) x -= Bq;
-      else if (Cq < 0) { x += Cq; cv = Bq + Cq; }
-      else cv = Bq;
-      if (cv) cap[(long long)st.rev[e] * g.NP + w] += cv;
-    }
+  *c0 += E0;
+  return E0 - E1;
+}
+
+// Edge-e share of node w (padded index): both ends' terms of direction e,
+// the capacity words of planes e and rev[e] at w (read-modify-write), the
+// own term's constant added to *c0.  Returns the excess share; *bad is set
+// for a non-submodular own term.
+template <bool VEC>
+__host__ __device__ __forceinline__ long long fill_gather_edge(
+    const Geo& g, const Stencil& st, long long r, int a, int b, int c, long long w, int e,
+    const int64_t* binary, long long* cap, bool* bad, long long* c0) {
+  const int Kp = st.K / 2;
+  const int da = st.da[e], db = st.db[e], dc = st.dc[e];
+  long long x = 0, A, B, C, D;
+  if (a + da >= 0 && a + da < g.A && b + db >= 0 && b + db < g.B && c + dc >= 0 &&
+      c + dc < g.C) {  // own term, w is its source end
+    fill_table<VEC>(binary, Kp, r, e, A, B, C, D);
+    *c0 += A;
+    const long long Bq = B - A, Cq = C - D;
+    if (Bq + Cq < 0) *bad = true;
+    long long cu = 0;
+    x += A - D;
+    if (Bq < 0) { x += Bq; cu = Bq + Cq; }
+    else if (Cq < 0) x -= Cq;
+    else cu = Cq;
+    if (cu) cap[(long long)e * g.NP + w] += cu;
   }
+  const int sa = a - da, sb = b - db, sc = c - dc;
+  if (sa >= 0 && sa < g.A && sb >= 0 && sb < g.B && sc >= 0 && sc < g.C) {  // w is the target
+    fill_table<VEC>(binary, Kp, ((long long)sa * g.B + sb) * g.C + sc, e, A, B, C, D);
+    const long long Bq = B - A, Cq = C - D;
+    long long cv = 0;
+    if (Bq < 0) x -= Bq;
+    else if (Cq < 0) { x += Cq; cv = Bq + Cq; }
+    else cv = Bq;
+    if (cv) cap[(long long)st.rev[e] * g.NP + w] += cv;
+  }
+  return x;
+}
+
+// All of node r: returns its share of the constant term.
+template <bool VEC>
+__host__ __device__ __forceinline__ long long fill_gather_node(
+    const Geo& g, const Stencil& st, long long r, int a, int b, int c, const int64_t* unary,
+    const int64_t* binary, long long* exc, long long* cap, bool* bad) {
+  const long long w = ((long long)a * g.Bp + b) * g.Cp + c;
+  long long c0 = 0;
+  long long x = fill_gather_unary<VEC>(unary, r, &c0);
+  for (int e = 0; e < st.K / 2; ++e)
+    x += fill_gather_edge<VEC>(g, st, r, a, b, c, w, e, binary, cap, bad, &c0);
   if (x) exc[w] += x;
   return c0;
 }
 
-// One thread per node (k_fill_energy's gather form): no atomics on the
-// accumulators.  Used for device-resident energies; pinned host energies read
-// in place keep the scatter, which reads each pairwise table once.
-template <bool VEC>
-__global__ void k_fill_energy_gather(Geo g, Stencil st, int nd, long long N,
-                                     const int64_t* unary, const int64_t* binary, long long* exc,
-                                     long long* cap, long long* c0sum, int* err) {
-  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long c0 = 0;
-  if (r < N) {
-    int a, b, c;
-    if (nd == 2) { a = 0; b = int(r / g.C); c = int(r % g.C); }
-    else { c = int(r % g.C); b = int((r / g.C) % g.B); a = int(r / ((long long)g.C * g.B)); }
-    bool bad = false;
-    c0 = fill_gather_node<VEC>(g, st, r, a, b, c, unary, binary, exc, cap, &bad);
-    if (bad) atomicExch(err, 1);
-  }
+__device__ __forceinline__ void fill_node_coords(const Geo& g, int nd, long long r, int& a, int& b,
+                                                 int& c) {
+  if (nd == 2) { a = 0; b = int(r / g.C); c = int(r % g.C); }
+  else { c = int(r % g.C); b = int((r / g.C) % g.B); a = int(r / ((long long)g.C * g.B)); }
+}
+
+// Block sum of the constant term, one atomic per block.
+__device__ __forceinline__ void fill_add_c0(long long c0, long long* c0sum) {
   __shared__ long long red[32];
   for (int o = 16; o > 0; o >>= 1) c0 += __shfl_down_sync(0xffffffffu, c0, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c0;
@@ -182,6 +197,56 @@ __global__ void k_fill_energy_gather(Geo g, Stencil st, int nd, long long N,
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (threadIdx.x == 0 && v) atom_add(c0sum, v);
   }
+}
+
+// One thread per node (k_fill_energy's gather form): no atomics on the
+// accumulators.  Used for device-resident energies whose Kp does not divide
+// a warp; pinned host energies read in place keep the scatter, which reads
+// each pairwise table once.
+template <bool VEC>
+__global__ void k_fill_energy_gather(Geo g, Stencil st, int nd, long long N,
+                                     const int64_t* unary, const int64_t* binary, long long* exc,
+                                     long long* cap, long long* c0sum, int* err) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long c0 = 0;
+  if (r < N) {
+    int a, b, c;
+    fill_node_coords(g, nd, r, a, b, c);
+    bool bad = false;
+    c0 = fill_gather_node<VEC>(g, st, r, a, b, c, unary, binary, exc, cap, &bad);
+    if (bad) atomicExch(err, 1);
+  }
+  fill_add_c0(c0, c0sum);
+}
+
+// The gather with one lane per filling edge: KP (a power of two, dividing
+// 32) adjacent lanes of a warp share node r = t / KP, lane e = t % KP takes
+// direction e, so a warp's own-table reads are one contiguous span; the
+// node's excess share is summed across its lanes with shuffles and written
+// by lane 0 of the group.  Same words, same writers per word as the node
+// form.
+template <bool VEC, int KP>
+__global__ void k_fill_energy_lanes(Geo g, Stencil st, int nd, long long N,
+                                    const int64_t* unary, const int64_t* binary, long long* exc,
+                                    long long* cap, long long* c0sum, int* err) {
+  static_assert(KP >= 1 && KP <= 32 && (32 % KP) == 0, "lanes per node must divide a warp");
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long r = t / KP;
+  const int e = int(t % KP);
+  long long c0 = 0, x = 0, w = 0;
+  if (r < N) {
+    int a, b, c;
+    fill_node_coords(g, nd, r, a, b, c);
+    w = ((long long)a * g.Bp + b) * g.Cp + c;
+    bool bad = false;
+    x = fill_gather_edge<VEC>(g, st, r, a, b, c, w, e, binary, cap, &bad, &c0);
+    if (e == 0) x += fill_gather_unary<VEC>(unary, r, &c0);
+    if (bad) atomicExch(err, 1);
+  }
+#pragma unroll
+  for (int o = KP / 2; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  if (r < N && e == 0 && x) exc[w] += x;
+  fill_add_c0(c0, c0sum);
 }
 
 // Capacity form: source = cost off, sink = cost on, edge = symmetric capacity.
@@ -353,11 +418,23 @@ static inline int nblk(long long n, int t) { return int((n + t - 1) / t); }
 
 cudaError_t launch_fill_energy(const Geo& g, const Stencil& st, int nd, long long N,
                                const int64_t* u, const int64_t* b, long long* exc,
-                               long long* cap, long long* c0, int* err, bool gather,
+                               long long* cap, long long* c0, int* err, int form,
                                cudaStream_t s) {
   long long n = N * (st.K / 2);
   const bool vec = (reinterpret_cast<uintptr_t>(u) % 16 == 0) && (reinterpret_cast<uintptr_t>(b) % 16 == 0);
-  if (gather && N > 0) {
+  // form: 0 = lanes (where Kp divides a warp, else per node), 1 = per node,
+  // 2 = scatter
+  const int Kp = st.K / 2;
+  const bool gather = form == 0 || form == 1;
+  if (form == 0 && N > 0 && (Kp == 2 || Kp == 4 || Kp == 8)) {
+#define LF_FILL_LANES(KP)                                                                      \
+  if (vec) k_fill_energy_lanes<true, KP><<<nblk(N * KP, 256), 256, 0, s>>>(g, st, nd, N, u, b, exc, cap, c0, err); \
+  else k_fill_energy_lanes<false, KP><<<nblk(N * KP, 256), 256, 0, s>>>(g, st, nd, N, u, b, exc, cap, c0, err);
+    if (Kp == 2) { LF_FILL_LANES(2) }
+    else if (Kp == 4) { LF_FILL_LANES(4) }
+    else { LF_FILL_LANES(8) }
+#undef LF_FILL_LANES
+  } else if (gather && N > 0) {
     if (vec) k_fill_energy_gather<true><<<nblk(N, 256), 256, 0, s>>>(g, st, nd, N, u, b, exc, cap, c0, err);
     else k_fill_energy_gather<false><<<nblk(N, 256), 256, 0, s>>>(g, st, nd, N, u, b, exc, cap, c0, err);
   } else if (n > 0) {

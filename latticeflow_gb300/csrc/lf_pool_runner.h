@@ -32,6 +32,10 @@ struct Tuning {
   int device_loops = 0;          // TMA-staged passes: 1 = device-side pass loops (CUDA
                                  // graphs with conditional nodes), 0 = one launch per
                                  // pass from the host
+  int fill_kernel = 0;           // energy fill of device-resident arrays: 0 = gathered, one
+                                 // lane per filling edge where K / 2 divides a warp (else
+                                 // per node), 1 = gathered per node, 2 = scattered with
+                                 // atomics (pinned host arrays read in place: always 2)
 };
 
 struct SolveStats {

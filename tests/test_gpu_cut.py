@@ -300,6 +300,50 @@ def test_tma_pass_full_size_all_variants(native, gpu, oracle_port):
         del L
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel,dims", [("Full2d_4", (70, 45)), ("Full2d_8", (44, 90)),
+                                         ("Star2d_16", (37, 50)), ("Full2d_12", (40, 41)),
+                                         ("Full3d_26", (9, 10, 37))])
+def test_fill_forms_agree(native, gpu, oracle_port, kernel, dims):
+    """The three forms of the energy fill for device arrays (fill_kernel 0:
+    one lane per filling edge where K/2 divides a warp, else one thread per
+    node; 1: one thread per node; 2: scattered with atomics), with 16-byte
+    aligned and unaligned arrays, give the oracle's minimum energy and cut
+    sets.  The pairwise tables are general submodular ones: B - A and C - D
+    take both signs, so every branch of the decomposition runs."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import _native as N
+    rng = np.random.default_rng(5)
+    n = int(np.prod(dims))
+    kp = len(oracle_port.lattice_offsets(kernel)[0]) // 2
+    u = rng.integers(-60, 61, size=(n, 2)).astype(np.int64)
+    A = rng.integers(-40, 41, size=(n, kp))
+    D = rng.integers(-40, 41, size=(n, kp))
+    x = rng.integers(-30, 61, size=(n, kp))
+    y = np.maximum(rng.integers(-30, 61, size=(n, kp)), -x)   # x + y >= 0: submodular
+    b = np.stack([A, A + x, D + y, D], axis=2).astype(np.int64)
+    E, cmin, cmax, _, _ = oracle_port.port_canonical(kernel, dims, u, b)
+    for form in (0, 1, 2):
+        for off in (0, 1):
+            ub = torch.zeros(u.size + 2, dtype=torch.int64, device="cuda")
+            bb = torch.zeros(b.size + 2, dtype=torch.int64, device="cuda")
+            uu = ub[off:off + u.size]
+            bv = bb[off:off + b.size]
+            uu.copy_(torch.from_numpy(u.reshape(-1)))
+            bv.copy_(torch.from_numpy(b.reshape(-1)))
+            torch.cuda.synchronize()
+            L = lf.LatticeFlow(kernel, "LatticeEnergyMinimizer", dims)
+            L.setParam("fill_kernel", form)
+            N.check(N.lib().lf_add_energy_potentials_device(L._h, ctypes.c_void_p(uu.data_ptr()),
+                                                            ctypes.c_void_p(bv.data_ptr())))
+            L.run()
+            assert L.flow()[1] == E, (form, off)
+            assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax), (form, off)
+
+
+@pytest.mark.gpu
 def test_unaligned_energy_arrays(native, gpu, oracle_port):
     """Device energy arrays that are 8- but not 16-byte aligned take the
     scalar fill (aligned ones the 16-byte vector fill); both give the
