@@ -92,6 +92,34 @@ def test_port_against_compiled_reference_random(oracle_port):
         assert O.energy(kernel, dims, u, b, pr) == E
 
 
+def test_port_against_compiled_reference_general_tables(oracle_port):
+    """General submodular pairwise tables (E01 - E00 and E10 - E11 of both
+    signs, so every branch of the reparametrisation runs,
+    network_flow_node.hpp:420-485), on the kernels and sizes of the GPU
+    fill-form test: the port's labellings and energy equal the compiled
+    reference's PR and BK solvers."""
+    O = oracle_port
+    if not O.ref_available():
+        pytest.skip("compiled reference not present")
+    for kernel, dims in [("Full2d_4", (70, 45)), ("Full2d_8", (44, 90)), ("Star2d_16", (37, 50)),
+                         ("Full2d_12", (40, 41)), ("Full3d_26", (9, 10, 37))]:
+        rng = np.random.default_rng(5)
+        n = int(np.prod(dims))
+        kp = len(O.lattice_offsets(kernel)[0]) // 2
+        u = rng.integers(-60, 61, size=(n, 2)).astype(np.int64)
+        A = rng.integers(-40, 41, size=(n, kp))
+        D = rng.integers(-40, 41, size=(n, kp))
+        x = rng.integers(-30, 61, size=(n, kp))
+        y = np.maximum(rng.integers(-30, 61, size=(n, kp)), -x)
+        b = np.stack([A, A + x, D + y, D], axis=2).astype(np.int64)
+        pr, _ = O.ref_solve("LatticeEnergyMinimizer", kernel, dims, u, b)
+        bk, _ = O.ref_solve("BKGCEnergyMinimizer", kernel, dims, u, b)
+        E, cmin, cmax, cpr, _ = O.port_canonical(kernel, dims, u, b)
+        assert np.array_equal(cpr, pr) and np.array_equal(cmin, bk), kernel
+        assert O.energy(kernel, dims, u, b, pr) == E, kernel
+        assert O.energy(kernel, dims, u, b, cmax) == E, kernel
+
+
 def test_port_tv_against_compiled_reference(oracle_port):
     O = oracle_port
     if not O.ref_available():
