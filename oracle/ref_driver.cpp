@@ -49,10 +49,11 @@ int run_solver(const size_t* dims, long* u, long* b, int* c, double* w, double* 
   return run_direct<S<nd, K, long>, nd>(dims, u, b, c, w, cp, fd);
 }
 
-#define LF_KERNEL_LIST(X)                                  \
-  X(2, Full2d_4) X(2, Full2d_8) X(2, Full2d_12) X(2, Star2d_16) \
-  X(2, Full2d_20) X(2, Full2d_24) X(3, Full3d_6) X(3, Full3d_18) \
-  X(3, Star3d_26)
+#define LF_KERNEL_LIST(X)                                                  \
+  X(2, Full2d_4) X(2, Full2d_8) X(2, Full2d_12) X(2, Star2d_16)               \
+  X(2, Full2d_20) X(2, Full2d_24) X(2, Star2d_24) X(2, Full2d_28)             \
+  X(2, Star2d_32) X(2, Full2d_36) X(2, Full2d_48) X(3, Full3d_6)              \
+  X(3, Full3d_18) X(3, Star3d_26) X(3, Full3d_32)
 
 template <template <int, typename, typename> class S>
 int dispatch(const std::string& kernel, const size_t* dims, long* u, long* b, int* c,

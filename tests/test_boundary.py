@@ -45,11 +45,13 @@ def test_registry_matches_compiled_reference_deltas(native, oracle_port):
     if not O.ref_available():
         pytest.skip("compiled reference not present")
     import latticeflow_gb300 as lf
-    for k, dims in [("Full2d_4", (5, 6)), ("Full2d_8", (5, 6)), ("Star2d_16", (7, 6)),
-                    ("Full3d_26", (4, 5, 6)), ("Full3d_6", (4, 4, 4))]:
+    names = lf.validKernelNames()
+    assert len(names) == 20
+    for k in names:  # every name, aliases included (the compiled reference holds them all)
+        dims = (9, 8) if lf.kernelDimension(k) == 2 else (5, 6, 7)
         d, _, _ = lf.kernelInfo(k)
         fd = O.ref_filling_deltas(k, dims)
-        assert np.array_equal(fd, d[: len(d) // 2])
+        assert np.array_equal(fd, d[: len(d) // 2]), k
 
 
 def test_names_validation(native):

@@ -120,6 +120,34 @@ def test_port_against_compiled_reference_general_tables(oracle_port):
         assert O.energy(kernel, dims, u, b, cmax) == E, kernel
 
 
+@pytest.mark.parametrize("kernel,dims", [
+    ("Full2d_4", (33, 65)), ("Full2d_8", (30, 31)), ("Full2d_12", (20, 21)), ("Star2d_16", (19, 25)),
+    ("Full2d_20", (17, 19)), ("Full2d_24", (18, 18)), ("Star2d_24", (17, 18)), ("Full2d_28", (16, 17)),
+    ("Star2d_32", (16, 18)), ("Full2d_36", (15, 17)), ("Full2d_48", (15, 16)), ("Full3d_6", (6, 7, 20)),
+    ("Full3d_18", (5, 6, 19)), ("Full3d_26", (6, 6, 17)), ("Full3d_32", (5, 6, 18))])
+def test_port_against_compiled_reference_every_kernel(oracle_port, kernel, dims):
+    """Every distinct kernel of the reference's default build, general
+    submodular tables: the port's labellings and energy equal the compiled
+    reference's PR and BK solvers."""
+    O = oracle_port
+    if not O.ref_available():
+        pytest.skip("compiled reference not present")
+    rng = np.random.default_rng(11)
+    n = int(np.prod(dims))
+    kp = len(O.lattice_offsets(kernel)[0]) // 2
+    u = rng.integers(-60, 61, size=(n, 2)).astype(np.int64)
+    A = rng.integers(-40, 41, size=(n, kp))
+    D = rng.integers(-40, 41, size=(n, kp))
+    x = rng.integers(-30, 61, size=(n, kp))
+    y = np.maximum(rng.integers(-30, 61, size=(n, kp)), -x)
+    b = np.stack([A, A + x, D + y, D], axis=2).astype(np.int64)
+    pr, _ = O.ref_solve("LatticeEnergyMinimizer", kernel, dims, u, b)
+    bk, _ = O.ref_solve("BKGCEnergyMinimizer", kernel, dims, u, b)
+    E, cmin, cmax, cpr, _ = O.port_canonical(kernel, dims, u, b)
+    assert np.array_equal(cpr, pr) and np.array_equal(cmin, bk)
+    assert O.energy(kernel, dims, u, b, pr) == E == O.energy(kernel, dims, u, b, cmax)
+
+
 def test_port_tv_against_compiled_reference(oracle_port):
     O = oracle_port
     if not O.ref_available():
