@@ -127,16 +127,16 @@ void Batch::check_err(const char* msg) {
 void Batch::add_caps(int i, const int32_t* src, const int32_t* snk, const int32_t* edge) {
   alloc_accumulators();
   Member& m = member(i);
-  int32_t* buf = nullptr;
   size_t nb = (size_t)m.N * sizeof(int32_t), eb = (size_t)m.N * (m.st.K / 2) * sizeof(int32_t);
-  check(cudaMallocAsync(&buf, 2 * nb + eb, stream), "cudaMallocAsync");
+  DevBuf<int32_t> stage;
+  stage.alloc((2 * nb + eb) / sizeof(int32_t), stream);
+  int32_t* buf = stage.p;
   int32_t *ds = nullptr, *dt = nullptr, *de = nullptr;
   if (src) { ds = buf; check(cudaMemcpyAsync(ds, src, nb, cudaMemcpyHostToDevice, stream), "memcpy"); }
   if (snk) { dt = buf + m.N; check(cudaMemcpyAsync(dt, snk, nb, cudaMemcpyHostToDevice, stream), "memcpy"); }
   if (edge) { de = buf + 2 * m.N; check(cudaMemcpyAsync(de, edge, eb, cudaMemcpyHostToDevice, stream), "memcpy"); }
   check(launch_fill_caps(m.g, m.st, m.nd, m.N, ds, dt, de, d_exc64 + m.node_base,
                          d_cap64 + m.res_base, d_c0 + i, d_err, 0, stream), "fill caps");
-  cudaFreeAsync(buf, stream);
   solved = false;
   if (!defer_checks) check_err("capacities must be non-negative");
 }
@@ -145,13 +145,13 @@ void Batch::add_energy(int i, const int64_t* unary, const int64_t* binary) {
   alloc_accumulators();
   Member& m = member(i);
   size_t ub = (size_t)m.N * 2 * sizeof(int64_t), bb = (size_t)m.N * (m.st.K / 2) * 4 * sizeof(int64_t);
-  int64_t* buf = nullptr;
-  check(cudaMallocAsync(&buf, ub + bb, stream), "cudaMallocAsync");
+  DevBuf<int64_t> stage;
+  stage.alloc((ub + bb) / sizeof(int64_t), stream);
+  int64_t* buf = stage.p;
   check(cudaMemcpyAsync(buf, unary, ub, cudaMemcpyHostToDevice, stream), "memcpy");
   check(cudaMemcpyAsync(buf + 2 * m.N, binary, bb, cudaMemcpyHostToDevice, stream), "memcpy");
   check(launch_fill_energy(m.g, m.st, m.nd, m.N, buf, buf + 2 * m.N, d_exc64 + m.node_base,
                            d_cap64 + m.res_base, d_c0 + i, d_err, tune.fill_kernel, stream), "fill energy");
-  cudaFreeAsync(buf, stream);
   solved = false;
   if (!defer_checks) check_err("pairwise term is not submodular (E00 + E11 > E01 + E10)");
 }
@@ -249,8 +249,9 @@ void Batch::fetch_cuts() {
   if (cuts_fetched) return;
   long long total = 0;
   for (Member& m : members) total += m.N;
-  int* buf = nullptr;
-  check(cudaMallocAsync(&buf, 2 * std::max<long long>(total, 1) * sizeof(int), stream), "cudaMallocAsync");
+  DevBuf<int> stage;
+  stage.alloc(2 * std::max<long long>(total, 1), stream);
+  int* buf = stage.p;
   long long off = 0;
   for (Member& m : members) {
     check(launch_extract_cuts(m.g, m.nd, m.N, d_mark + m.node_base, d_h + m.node_base, buf + off,
@@ -259,7 +260,6 @@ void Batch::fetch_cuts() {
   }
   host_cuts.resize(2 * total);
   check(cudaMemcpyAsync(host_cuts.data(), buf, 2 * total * sizeof(int), cudaMemcpyDeviceToHost, stream), "memcpy");
-  cudaFreeAsync(buf, stream);
   check(cudaStreamSynchronize(stream), "sync");
   off = 0;
   for (Member& m : members) {

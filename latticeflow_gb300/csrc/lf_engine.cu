@@ -196,7 +196,7 @@ static const void* mapped_host_ptr(const void* p) {
 void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device_ptrs) {
   alloc_accumulators();
   const int64_t *du = unary, *db = binary;
-  int64_t *tu = nullptr, *tb = nullptr;
+  DevBuf<int64_t> tu, tb;  // staging copies of pageable arrays
   size_t ub = (size_t)N * 2 * sizeof(int64_t), bb = (size_t)N * (st.K / 2) * 4 * sizeof(int64_t);
   // pinned caller arrays: the fill kernel reads them in place, so the
   // transfer overlaps the fill instead of preceding it
@@ -209,12 +209,12 @@ void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device
     device_ptrs = true;
   }
   if (!device_ptrs) {
-    check(cudaMallocAsync(&tu, ub, stream), "cudaMallocAsync unary");
-    check(cudaMallocAsync(&tb, bb, stream), "cudaMallocAsync binary");
-    check(cudaMemcpyAsync(tu, unary, ub, cudaMemcpyHostToDevice, stream), "memcpy unary");
-    check(cudaMemcpyAsync(tb, binary, bb, cudaMemcpyHostToDevice, stream), "memcpy binary");
-    du = tu;
-    db = tb;
+    tu.alloc(ub / sizeof(int64_t), stream);
+    tb.alloc(bb / sizeof(int64_t), stream);
+    check(cudaMemcpyAsync(tu.p, unary, ub, cudaMemcpyHostToDevice, stream), "memcpy unary");
+    check(cudaMemcpyAsync(tb.p, binary, bb, cudaMemcpyHostToDevice, stream), "memcpy binary");
+    du = tu.p;
+    db = tb.p;
   }
   if (parametric)  // the reference's 2x-scaled reparametrisation (network_flow_node.hpp:420-485)
     check(counted(launch_fill_energy_pf(g, st, nd, N, du, db, d_exc64, d_cap64, d_err, stream)),
@@ -224,8 +224,6 @@ void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device
                                           in_place ? 2 : tune.fill_kernel,
                                           stream)),
           "fill energy");
-  if (tu) cudaFreeAsync(tu, stream);
-  if (tb) cudaFreeAsync(tb, stream);
   int err = 0;
   sync_read(&err, d_err, sizeof(int));
   if (err) throw LfError{3, "pairwise term is not submodular (E00 + E11 > E01 + E10)"};
@@ -234,9 +232,10 @@ void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device
 
 void Engine::add_caps(const int32_t* src, const int32_t* snk, const int32_t* edge) {
   alloc_accumulators();
-  int32_t* buf = nullptr;
   size_t nb = (size_t)N * sizeof(int32_t), eb = (size_t)N * (st.K / 2) * sizeof(int32_t);
-  check(cudaMallocAsync(&buf, 2 * nb + eb, stream), "cudaMallocAsync caps");
+  DevBuf<int32_t> stage;  // staging copies of pageable arrays
+  stage.alloc((2 * nb + eb) / sizeof(int32_t), stream);
+  int32_t* buf = stage.p;
   int32_t *ds = nullptr, *dt = nullptr, *de = nullptr;
   // pinned caller arrays are read in place (see add_energy)
   auto in = [&](const int32_t* h, int32_t* stage, size_t bytes) -> int32_t* {
@@ -251,7 +250,6 @@ void Engine::add_caps(const int32_t* src, const int32_t* snk, const int32_t* edg
   check(counted(launch_fill_caps(g, st, nd, N, ds, dt, de, d_exc64, d_cap64, d_c0, d_err,
                                  parametric ? 1 : 0, stream)),
         "fill caps");
-  cudaFreeAsync(buf, stream);
   int err = 0;
   sync_read(&err, d_err, sizeof(int));
   if (err) throw LfError{3, "capacities must be non-negative"};

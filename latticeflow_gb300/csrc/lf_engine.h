@@ -13,6 +13,25 @@
 
 namespace lfg {
 
+// Stream-ordered temporary device buffer (no device-wide synchronisation,
+// so concurrent solves on other streams keep running), freed in stream order
+// when it goes out of scope, on error paths too.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  cudaStream_t s = nullptr;
+  void alloc(size_t count, cudaStream_t st) {
+    s = st;
+    cudaError_t e = cudaMallocAsync(&p, count * sizeof(T), st);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw LfError{e == cudaErrorMemoryAllocation ? 5 : 6,
+                    std::string("cudaMallocAsync: ") + cudaGetErrorString(e)};
+    }
+  }
+  ~DevBuf() { if (p) cudaFreeAsync(p, s); }
+};
+
 // per-lattice element kernels (lf_kernels.cu)
 cudaError_t launch_fill_energy(const Geo& g, const Stencil& st, int nd, long long N,
                                const int64_t* u, const int64_t* b, long long* exc, long long* cap,

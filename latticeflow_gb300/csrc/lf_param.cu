@@ -208,24 +208,6 @@ __global__ void k_pf_levels(Geo g, int nd, long long N, const long long* exc, in
   r[b] = -exc[((long long)a * g.Bp + bb) * g.Cp + c];
 }
 
-// Stream-ordered temporary device buffer (no device-wide synchronisation,
-// so concurrent solves on other streams keep running).
-template <class T>
-struct DevBuf {
-  T* p = nullptr;
-  cudaStream_t s = nullptr;
-  void alloc(size_t count, cudaStream_t st) {
-    s = st;
-    cudaError_t e = cudaMallocAsync(&p, count * sizeof(T), st);
-    if (e != cudaSuccess) {
-      p = nullptr;
-      throw LfError{e == cudaErrorMemoryAllocation ? 5 : 6,
-                    std::string("cudaMallocAsync: ") + cudaGetErrorString(e)};
-    }
-  }
-  ~DevBuf() { if (p) cudaFreeAsync(p, s); }
-};
-
 }  // namespace
 
 cudaError_t launch_fill_energy_pf(const Geo& g, const Stencil& st, int nd, long long N,
