@@ -60,3 +60,33 @@ def test_single_process_is_its_own_max():
     import bench
     assert bench.max_over_ranks(3.25) == 3.25
     assert bench.replica_value(7, 1, 2.0) == 3.5
+
+
+def test_run_split_spreads_steps_and_overlaps_blocking_calls():
+    """bench.run_split: `steps` calls spread round robin over the handles'
+    threads, the threads overlapping calls that block outside the
+    interpreter (as the engine's C calls do), and an error in one thread
+    raised on the caller."""
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+    calls = [0, 0, 0]
+
+    def make(j):
+        def step():
+            calls[j] += 1
+            time.sleep(0.02)
+            return j
+        return step
+
+    t0 = time.perf_counter()
+    assert bench.run_split([make(0), make(1), make(2)], 10) == 0
+    wall = time.perf_counter() - t0
+    assert calls == [4, 3, 3]
+    assert wall < 0.15   # 4 sleeps of 20 ms in sequence at most, not 10
+
+    def bad():
+        raise RuntimeError("engine error")
+
+    with pytest.raises(RuntimeError, match="engine error"):
+        bench.run_split([make(0), bad], 6)
