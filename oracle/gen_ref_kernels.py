@@ -16,7 +16,7 @@ import kernels  # noqa: E402
 
 
 def main(out_dir):
-    specs = kernels.generate()
+    specs = kernels.generate(optional=True)  # the default build plus --1d and --4d
     body = []
     for name, s in specs.items():
         if s.alias_of:
@@ -33,7 +33,7 @@ def main(out_dir):
     os.makedirs(d, exist_ok=True)
     with open(os.path.join(d, "kernels.hpp"), "w") as f:
         f.write("// generated by oracle/gen_ref_kernels.py (oracle build only)\n")
-        f.write("#ifndef _KERNELS_H_\n#define _KERNELS_H_\n#define MAX_KERNEL_DIMENSION 3\n")
+        f.write("#ifndef _KERNELS_H_\n#define _KERNELS_H_\n#define MAX_KERNEL_DIMENSION 4\n")
         f.write('#include "kernels/kernel_base.hpp"\nnamespace latticeQBP {\n')
         f.write("\n".join(body))
         f.write("\n}\n#endif\n")

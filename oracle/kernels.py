@@ -31,6 +31,12 @@ from itertools import product
 
 # default radii: wscript:54-64 (2-d: 4, 3-d: 2) with code_setup.py:13
 DEFAULT_MAX_RADIUS = {2: 4, 3: 2}
+# opt-in dimensions of the reference build (options and defaults at
+# wscript:49-67): --1d adds Full kernels at the integer radii
+# 1 .. max_1d_radius - 1 (code_setup.py:81-92), --4d Full and Star kernels at
+# the 4-d radius intervals up to max_4d_radius (code_setup.py:135-153)
+OPTIONAL_1D_MAX_RADIUS = 8
+OPTIONAL_4D_MAX_RADIUS = 1
 
 
 def radius_intervals(dim, max_radius):
@@ -121,32 +127,40 @@ class KernelSpec:
         return offs, [wmap[o] for o in offs]
 
 
-def generate(max_radius=None):
-    """All kernel specs, keyed by name, in generation order."""
+def generate(max_radius=None, optional=False):
+    """All kernel specs, keyed by name, in generation order.  optional: also
+    the kernels of the reference's opt-in 1-d and 4-d builds (--1d, --4d)."""
     if max_radius is None:
         max_radius = DEFAULT_MAX_RADIUS
     specs = {}
     seen_sets = {}
-    for dim in sorted(max_radius):
-        for r in radius_intervals(dim, max_radius[dim]):
-            for kind in ("Full", "Star"):
-                offs = full_offsets(dim, r) if kind == "Full" else star_offsets(dim, r)
-                if not offs:
-                    continue
-                name = "%s%dd_%d" % (kind, dim, len(offs))
-                key = frozenset(offs)
-                if key in seen_sets:
-                    if name in specs:
-                        continue
-                    base = specs[seen_sets[key]]
-                    specs[name] = KernelSpec(name, kind, dim, r, base.offsets,
-                                             base.geocut, base.weights, alias_of=base.name)
-                    continue
+
+    def add(dim, r, kinds):
+        for kind in kinds:
+            offs = full_offsets(dim, r) if kind == "Full" else star_offsets(dim, r)
+            if not offs:
+                continue
+            name = "%s%dd_%d" % (kind, dim, len(offs))
+            key = frozenset(offs)
+            if key in seen_sets:
                 if name in specs:
                     continue
-                g, w = geocut_weights(dim, offs)
-                specs[name] = KernelSpec(name, kind, dim, r, offs, g, w)
-                seen_sets[key] = name
+                base = specs[seen_sets[key]]
+                specs[name] = KernelSpec(name, kind, dim, r, base.offsets,
+                                         base.geocut, base.weights, alias_of=base.name)
+                continue
+            if name in specs:
+                continue
+            g, w = geocut_weights(dim, offs)
+            specs[name] = KernelSpec(name, kind, dim, r, offs, g, w)
+            seen_sets[key] = name
+
+    if optional:
+        for r in range(1, OPTIONAL_1D_MAX_RADIUS):
+            add(1, r, ("Full",))
+    for dim in sorted(max_radius):
+        for r in radius_intervals(dim, max_radius[dim]):
+            add(dim, r, ("Full", "Star"))
     # The full 3x3x3 neighbourhood comes out of the Star rule at radius 2
     # (Full3d_32 minus the six length-2 axis offsets) as "Star3d_26"; the name
     # "Full3d_26" is registered as an alias of it (code_setup.py:369-399
@@ -160,6 +174,9 @@ def generate(max_radius=None):
     else:
         specs["Full3d_26"] = KernelSpec("Full3d_26", "Full", 3, 2.0, offs26,
                                         False, [1.0] * 26)
+    if optional:
+        for r in radius_intervals(4, OPTIONAL_4D_MAX_RADIUS):
+            add(4, r, ("Full", "Star"))
     return specs
 
 

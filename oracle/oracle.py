@@ -27,6 +27,7 @@ REF_SO = os.path.join(HERE, "_ref", "libref_oracle.so")
 REF_SRC = "/root/reference/solver"
 
 _SPECS = None
+_ALL_SPECS = None
 _port = None
 _ref = None
 
@@ -38,9 +39,17 @@ def specs():
     return _SPECS
 
 
+def all_specs():
+    """specs() plus the kernels of the reference's opt-in 1-d and 4-d builds."""
+    global _ALL_SPECS
+    if _ALL_SPECS is None:
+        _ALL_SPECS = _kernels.generate(optional=True)
+    return _ALL_SPECS
+
+
 def lattice_offsets(kernel):
     """(offsets[K][nd], weights[K]) in lattice order (kernellattice.hpp:61-96)."""
-    s = specs()[kernel]
+    s = all_specs()[kernel]
     offs, w = s.lattice_order()
     return np.asarray(offs, dtype=np.int32), np.asarray(w, dtype=np.float64)
 
@@ -53,7 +62,8 @@ def build_ref():
     """Builds the compiled-reference oracle; returns False without sources."""
     if not os.path.isdir(REF_SRC):
         return False
-    subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
+    jobs = "-j%d" % max(1, min(5, os.cpu_count() or 1))  # the five parts of the driver at once
+    subprocess.run(["make", "-s", jobs, "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
     return True
 
 

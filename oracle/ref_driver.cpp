@@ -49,28 +49,69 @@ int run_solver(const size_t* dims, long* u, long* b, int* c, double* w, double* 
   return run_direct<S<nd, K, long>, nd>(dims, u, b, c, w, cp, fd);
 }
 
-#define LF_KERNEL_LIST(X)                                                  \
-  X(2, Full2d_4) X(2, Full2d_8) X(2, Full2d_12) X(2, Star2d_16)               \
-  X(2, Full2d_20) X(2, Full2d_24) X(2, Star2d_24) X(2, Full2d_28)             \
-  X(2, Star2d_32) X(2, Full2d_36) X(2, Full2d_48) X(3, Full3d_6)              \
-  X(3, Full3d_18) X(3, Star3d_26) X(3, Full3d_32)
+}  // namespace
 
+// The kernel instantiations are split over four translation units, compiled
+// in parallel from this file with -DLF_REF_PART=1..4; part 0 holds the C
+// entry points and the TV functions.  Solver ids: 0 LatticeEnergyMinimizer,
+// 1 BKGCEnergyMinimizer, 2 LatticeLevelReductions.
+#define LF_KERNELS_1(X) X(2, Full2d_4) X(2, Full2d_8) X(2, Full2d_12) X(2, Star2d_16) \
+                        X(1, Full1d_2) X(1, Full1d_4)
+#define LF_KERNELS_2(X) X(2, Full2d_20) X(2, Full2d_24) X(2, Star2d_24) X(2, Full2d_28) \
+                        X(1, Full1d_6) X(1, Full1d_8)
+#define LF_KERNELS_3(X) X(2, Star2d_32) X(2, Full2d_36) X(2, Full2d_48) X(1, Full1d_10) \
+                        X(1, Full1d_12)
+#define LF_KERNELS_4(X) X(3, Full3d_6) X(3, Full3d_18) X(3, Star3d_26) X(3, Full3d_32) \
+                        X(1, Full1d_14) X(4, Full4d_8)
+
+#define LF_PART_DECL(N)                                                                   \
+  int lf_ref_part_##N(int solver, const std::string& k, const size_t* dims, long* u, long* b, \
+                      int* c, double* w, double* cp, int* fd)
+LF_PART_DECL(1);
+LF_PART_DECL(2);
+LF_PART_DECL(3);
+LF_PART_DECL(4);
+
+#if defined(LF_REF_PART) && LF_REF_PART >= 1
+#if LF_REF_PART == 1
+#define LF_KERNELS LF_KERNELS_1
+#elif LF_REF_PART == 2
+#define LF_KERNELS LF_KERNELS_2
+#elif LF_REF_PART == 3
+#define LF_KERNELS LF_KERNELS_3
+#else
+#define LF_KERNELS LF_KERNELS_4
+#endif
+
+namespace {
 template <template <int, typename, typename> class S>
-int dispatch(const std::string& kernel, const size_t* dims, long* u, long* b, int* c,
-             double* w, double* cp, int* fd) {
-  std::string k = kernel;
-  if (k == "Full3d_26") k = "Star3d_26";
-  if (k == "Star2d_4") k = "Full2d_4";
-  if (k == "Star2d_8") k = "Full2d_8";
-  if (k == "Star3d_6") k = "Full3d_6";
-  if (k == "Star3d_18") k = "Full3d_18";
+int dispatch(const std::string& k, const size_t* dims, long* u, long* b, int* c, double* w,
+             double* cp, int* fd) {
 #define X(ND, KN) if (k == #KN) return run_solver<S, ND, KN>(dims, u, b, c, w, cp, fd);
-  LF_KERNEL_LIST(X)
+  LF_KERNELS(X)
 #undef X
   return -1;
 }
-
 }  // namespace
+
+#define LF_PART_DEF(N)                                                                 \
+  LF_PART_DECL(N) {                                                                     \
+    if (solver == 0) return dispatch<LatticeEnergyMinimizer>(k, dims, u, b, c, w, cp, fd); \
+    if (solver == 1) return dispatch<BKGCEnergyMinimizer>(k, dims, u, b, c, w, cp, fd);    \
+    if (solver == 2) return dispatch<LatticeLevelReductions>(k, dims, u, b, c, w, cp, fd); \
+    return -1;                                                                          \
+  }
+#if LF_REF_PART == 1
+LF_PART_DEF(1)
+#elif LF_REF_PART == 2
+LF_PART_DEF(2)
+#elif LF_REF_PART == 3
+LF_PART_DEF(3)
+#else
+LF_PART_DEF(4)
+#endif
+
+#else  // part 0: the C entry points
 
 extern "C" {
 
@@ -81,12 +122,20 @@ int ref_solve(const char* solver, const char* kernel, const size_t* dims,
               long* unary, long* binary, int* cut_out, double* wall_s,
               double* cpu_s, int* filling_deltas) {
   std::string s(solver);
-  if (s == "LatticeEnergyMinimizer")
-    return dispatch<LatticeEnergyMinimizer>(kernel, dims, unary, binary, cut_out, wall_s, cpu_s, filling_deltas);
-  if (s == "BKGCEnergyMinimizer")
-    return dispatch<BKGCEnergyMinimizer>(kernel, dims, unary, binary, cut_out, wall_s, cpu_s, filling_deltas);
-  if (s == "LatticeLevelReductions")
-    return dispatch<LatticeLevelReductions>(kernel, dims, unary, binary, cut_out, wall_s, cpu_s, filling_deltas);
+  const int id = s == "LatticeEnergyMinimizer" ? 0 : s == "BKGCEnergyMinimizer" ? 1
+               : s == "LatticeLevelReductions" ? 2 : -1;
+  if (id < 0) return -1;
+  std::string k(kernel);
+  if (k == "Full3d_26") k = "Star3d_26";
+  if (k == "Star2d_4") k = "Full2d_4";
+  if (k == "Star2d_8") k = "Full2d_8";
+  if (k == "Star3d_6") k = "Full3d_6";
+  if (k == "Star3d_18") k = "Full3d_18";
+  if (k == "Star4d_8") k = "Full4d_8";
+  for (auto part : {lf_ref_part_1, lf_ref_part_2, lf_ref_part_3, lf_ref_part_4}) {
+    const int r = part(id, k, dims, unary, binary, cut_out, wall_s, cpu_s, filling_deltas);
+    if (r >= 0) return r;
+  }
   return -1;
 }
 
@@ -127,3 +176,5 @@ int ref_tv_path(const char* kernel, size_t nx, size_t ny, double* f, int nl,
 }
 
 }  // extern "C"
+
+#endif  // LF_REF_PART

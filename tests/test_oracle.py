@@ -28,8 +28,21 @@ def test_kernel_generator_names_and_sizes():
     assert specs["Star2d_4"].alias_of == "Full2d_4"
 
 
+def test_kernel_generator_optional_dimensions():
+    """The reference's opt-in builds: --1d gives Full1d_2 .. Full1d_14 (integer
+    radii 1-7, Full only), --4d gives Full4d_8 with Star4d_8 as its alias;
+    the default set is unchanged by them."""
+    default = K.generate()
+    specs = K.generate(optional=True)
+    extra = [n for n in specs if n not in default]
+    assert extra == ["Full1d_%d" % (2 * r) for r in range(1, 8)] + ["Full4d_8", "Star4d_8"]
+    assert [n for n in specs if n in default] == list(default)
+    assert specs["Full1d_6"].offsets == [(-3,), (-2,), (-1,), (1,), (2,), (3,)]
+    assert specs["Star4d_8"].alias_of == "Full4d_8" and specs["Full4d_8"].size == 8
+
+
 def test_kernel_lattice_order_reverse_pairs():
-    for name, s in K.generate().items():
+    for name, s in K.generate(optional=True).items():
         offs, w = s.lattice_order()
         k = len(offs)
         for i in range(k // 2):
@@ -135,6 +148,35 @@ def test_port_against_compiled_reference_every_kernel(oracle_port, kernel, dims)
     rng = np.random.default_rng(11)
     n = int(np.prod(dims))
     kp = len(O.lattice_offsets(kernel)[0]) // 2
+    u = rng.integers(-60, 61, size=(n, 2)).astype(np.int64)
+    A = rng.integers(-40, 41, size=(n, kp))
+    D = rng.integers(-40, 41, size=(n, kp))
+    x = rng.integers(-30, 61, size=(n, kp))
+    y = np.maximum(rng.integers(-30, 61, size=(n, kp)), -x)
+    b = np.stack([A, A + x, D + y, D], axis=2).astype(np.int64)
+    pr, _ = O.ref_solve("LatticeEnergyMinimizer", kernel, dims, u, b)
+    bk, _ = O.ref_solve("BKGCEnergyMinimizer", kernel, dims, u, b)
+    E, cmin, cmax, cpr, _ = O.port_canonical(kernel, dims, u, b)
+    assert np.array_equal(cpr, pr) and np.array_equal(cmin, bk)
+    assert O.energy(kernel, dims, u, b, pr) == E == O.energy(kernel, dims, u, b, cmax)
+
+
+@pytest.mark.parametrize("kernel,dims", [
+    ("Full1d_2", (500,)), ("Full1d_4", (400,)), ("Full1d_6", (300,)), ("Full1d_8", (300,)),
+    ("Full1d_10", (250,)), ("Full1d_12", (250,)), ("Full1d_14", (200,)),
+    ("Full4d_8", (5, 6, 7, 8)), ("Star4d_8", (4, 5, 6, 7))])
+def test_port_against_compiled_reference_optional_kernels(oracle_port, kernel, dims):
+    """The kernels of the reference's opt-in 1-d and 4-d builds: offset
+    tables equal the compiled reference's edgeDeltas(), and the port's
+    labellings and energy equal its PR and BK solvers on general tables."""
+    O = oracle_port
+    if not O.ref_available():
+        pytest.skip("compiled reference not present")
+    rng = np.random.default_rng(13)
+    n = int(np.prod(dims))
+    offs = O.lattice_offsets(kernel)[0]
+    kp = len(offs) // 2
+    assert np.array_equal(O.ref_filling_deltas(kernel, dims), offs[:kp])
     u = rng.integers(-60, 61, size=(n, 2)).astype(np.int64)
     A = rng.integers(-40, 41, size=(n, kp))
     D = rng.integers(-40, 41, size=(n, kp))
