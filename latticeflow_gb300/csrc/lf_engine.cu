@@ -233,9 +233,9 @@ void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device
 void Engine::add_caps(const int32_t* src, const int32_t* snk, const int32_t* edge) {
   alloc_accumulators();
   size_t nb = (size_t)N * sizeof(int32_t), eb = (size_t)N * (st.K / 2) * sizeof(int32_t);
-  DevBuf<int32_t> stage;  // staging copies of pageable arrays
-  stage.alloc((2 * nb + eb) / sizeof(int32_t), stream);
-  int32_t* buf = stage.p;
+  DevBuf<int32_t> staging;  // staging copies of pageable arrays
+  staging.alloc((2 * nb + eb) / sizeof(int32_t), stream);
+  int32_t* buf = staging.p;
   int32_t *ds = nullptr, *dt = nullptr, *de = nullptr;
   // pinned caller arrays are read in place (see add_energy)
   auto in = [&](const int32_t* h, int32_t* stage, size_t bytes) -> int32_t* {
