@@ -41,6 +41,23 @@ def test_kernel_generator_optional_dimensions():
     assert specs["Star4d_8"].alias_of == "Full4d_8" and specs["Full4d_8"].size == 8
 
 
+def test_reference_driver_instantiates_every_distinct_kernel():
+    """oracle/ref_driver.cpp instantiates the reference solvers for exactly
+    the distinct (non-alias) kernels the generator gives, default and opt-in,
+    and maps every alias name onto its base."""
+    import re
+    src = open(os.path.join(os.path.dirname(GOLD), "..", "oracle", "ref_driver.cpp")).read()
+    listed = re.findall(r"X\((\d), (\w+)\)", src)
+    specs = K.generate(optional=True)
+    base = {n: s for n, s in specs.items() if not s.alias_of and n != "Full3d_26"}
+    assert sorted(n for _, n in listed) == sorted(base)
+    for nd, n in listed:
+        assert int(nd) == base[n].dim, n
+    for n, s in specs.items():
+        if s.alias_of:
+            assert 'k == "%s") k = "%s"' % (n, s.alias_of) in src, n
+
+
 def test_kernel_lattice_order_reverse_pairs():
     for name, s in K.generate(optional=True).items():
         offs, w = s.lattice_order()
