@@ -61,7 +61,7 @@ def parse():
                     help="one launch per pass (the default; kept for the recorded profiling commands)")
     ap.add_argument("--device-loops", action="store_true",
                     help="run the staged passes in device-side loops (CUDA graphs with conditional "
-                         "nodes, whose kernels a profiler does not list)")
+                         "nodes, whose kernels a profiler does not list); one handle only")
     ap.add_argument("--e2e-handles", type=int, default=1,
                     help="e2e with this many handles (own streams, own host threads) solving "
                          "concurrently, so one solve's host-to-device fill overlaps another's solve; "
@@ -69,7 +69,11 @@ def parse():
     ap.add_argument("--tuning", default=None,
                     help="tile_rows,local_sweeps,launches_per_relabel instead of the autotuner "
                          "(e.g. the setting a bench run chose, for a profile run)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.device_loops and args.e2e_handles > 1:
+        # device-side loops run on one handle and one host thread only
+        ap.error("--device-loops takes one handle: it cannot be combined with --e2e-handles > 1")
+    return args
 
 
 def dist_info():
@@ -338,8 +342,6 @@ def run_ours(args):
         extra = []
         for _ in range(args.e2e_handles - 1):
             Lx = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
-            if args.device_loops and not args.host_loops:
-                Lx.setParam("device_loops", 1)
             for k_, v_ in (tuning or {}).items():
                 Lx.setParam(k_, v_)
             cx = torch.empty(p.n, dtype=torch.int32).pin_memory()

@@ -239,12 +239,13 @@ int lf_server_group_stats(lf_server* s, int64_t* groups, int64_t* grouped);
  * (as lf_get_cut), flow_energy[2] the flow value and the minimum energy.
  * All intermediate state lives in one static device array of 8.5 MiB per GPU,
  * enough for 65,536 padded nodes (sides rounded up to 32, e.g. 256 x 256);
- * larger lattices return LF_ERR_RANGE.  The first call on a device looks the
- * array's address up (make that first call before any stream capture).  The
- * array is shared by all calls and keeps the last call's contents; each call
- * clears what must start at zero.  Calls whose GPU work overlapped would race
- * on it: the call holds a process-wide lock and synchronises `stream` (a
- * cudaStream_t, NULL = legacy default stream) before returning. */
+ * larger lattices return LF_ERR_RANGE.  Every call looks the array's device
+ * address up; the first call on a device also loads the array there (make
+ * that first call before any stream capture).  The array is shared by all
+ * calls and keeps the last call's contents; each call clears what must start
+ * at zero.  Calls whose GPU work overlapped would race on it: the call holds
+ * a process-wide lock and synchronises `stream` (a cudaStream_t, NULL =
+ * legacy default stream) before returning, on error returns too. */
 int lf_cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* source_device,
                       const int32_t* sink_device, const int32_t* edge_device,
                       int32_t* cut_device, int64_t* flow_energy_device, void* stream);

@@ -15,9 +15,12 @@
 // for the whole call and synchronises the caller's stream before it returns,
 // so calls from one process never overlap.
 //
-// The device address of the array is looked up once per device, with that
-// device current, by the first call made on it (cudaGetSymbolAddress); make
-// that first call before any stream capture.
+// Host code cannot use the array's name as a device address, so every call
+// looks the address up (cudaGetSymbolAddress) with the caller's device
+// current.  The first call on a device also loads the array's module there:
+// make that first call before any stream capture.  Looking the address up on
+// every call, instead of caching it, keeps it right after a cudaDeviceReset
+// or any other change of the device's primary context.
 #include <climits>
 #include <cstring>
 #include <mutex>
@@ -39,7 +42,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 namespace {
 
 std::mutex g_noalloc_lock;
-void* g_noalloc_base[256] = {nullptr};  // device address of the array, per device
 
 __global__ void k_noalloc_finish(const long long* supply, const long long* stuck,
                                  const long long* c0, int64_t* out) {
@@ -72,6 +74,14 @@ void read_back(T* host, const T* dev, cudaStream_t s) {
 
 }  // namespace
 
+namespace {
+
+void cut_2d_noalloc_locked(const KernelDef* kd, size_t nx, size_t ny, const int32_t* src,
+                           const int32_t* snk, const int32_t* edge, int32_t* cut,
+                           int64_t* flow_energy, cudaStream_t s);
+
+}  // namespace
+
 int cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* src,
                    const int32_t* snk, const int32_t* edge, int32_t* cut, int64_t* flow_energy,
                    cudaStream_t s) {
@@ -85,6 +95,23 @@ int cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* src,
   if (nx == 0 || ny == 0) throw LfError{LF_ERR_SHAPE, "empty lattice"};
   if (nx > (size_t)INT_MAX / 2 || ny > (size_t)INT_MAX / 2)
     throw LfError{LF_ERR_RANGE, "lattice extent too large"};
+  std::lock_guard<std::mutex> guard(g_noalloc_lock);
+  try {
+    cut_2d_noalloc_locked(kd, nx, ny, src, snk, edge, cut, flow_energy, s);
+  } catch (...) {
+    // work of this call that is still queued on `s` uses the shared array:
+    // let it finish before the lock lets the next call in
+    cudaStreamSynchronize(s);
+    throw;
+  }
+  return LF_OK;
+}
+
+namespace {
+
+void cut_2d_noalloc_locked(const KernelDef* kd, size_t nx, size_t ny, const int32_t* src,
+                           const int32_t* snk, const int32_t* edge, int32_t* cut,
+                           int64_t* flow_energy, cudaStream_t s) {
   const Stencil st = make_stencil(kd);
   Geo g{};
   const size_t dims[2] = {nx, ny};
@@ -96,18 +123,13 @@ int cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* src,
   const long long N = (long long)nx * (long long)ny;
   const int K = st.K;
 
-  std::lock_guard<std::mutex> guard(g_noalloc_lock);
-  int dev = 0;
-  ok(cudaGetDevice(&dev), "cudaGetDevice");
-  if (dev < 0 || dev >= 256) throw LfError{LF_ERR_CUDA, "device index out of range"};
-  if (!g_noalloc_base[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
+  void* base = nullptr;  // the array's address on the current device
+  {
+    cudaError_t e = cudaGetSymbolAddress(&base, g_noalloc_scratch);
+    if (e != cudaSuccess || !base)
       throw LfError{LF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)};
-    g_noalloc_base[dev] = p;
   }
-  Carve c{static_cast<unsigned char*>(g_noalloc_base[dev]), 0, kNoAllocScratchBytes};
+  Carve c{static_cast<unsigned char*>(base), 0, kNoAllocScratchBytes};
   long long* exc64 = c.take<long long>(g.NP);
   long long* cap64 = c.take<long long>((size_t)K * g.NP);
   int* res = c.take<int>((size_t)K * g.NP);
@@ -246,7 +268,8 @@ int cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* src,
   ok(cudaGetLastError(), "finish");
   ok(launch_extract_cuts(g, 2, N, mark, h, cut, nullptr, s), "extract cut");
   ok(cudaStreamSynchronize(s), "stream sync");
-  return LF_OK;
 }
+
+}  // namespace
 
 }  // namespace lfg

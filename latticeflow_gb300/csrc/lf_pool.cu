@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 
 #include "lf_pool_runner.h"
@@ -635,9 +636,35 @@ unsigned long long PoolRunner::activate(const T* exc, const int* h) {
   return total;
 }
 
+// Solves with device-side pass loops run one at a time in the process: the
+// loops stay single-threaded by construction (they are opt-in, and a GPU
+// fault was once seen with eight host threads each running their own loop
+// graphs at once).  The lock is held until the solve's work on the stream
+// has finished, on error paths too.
+namespace {
+std::mutex g_device_loop_lock;
+}
+
 template <typename T>
 void PoolRunner::maxflow(T* res, T* exc, int* h, uint64_t* mask, const uint64_t* kmask, int* markv,
                          SolveStats& stats, bool sets) {
+  if (tune.device_loops != 1) {
+    maxflow_epochs<T>(res, exc, h, mask, kmask, markv, stats, sets);
+    return;
+  }
+  std::lock_guard<std::mutex> lk(g_device_loop_lock);
+  try {
+    maxflow_epochs<T>(res, exc, h, mask, kmask, markv, stats, sets);
+  } catch (...) {
+    cudaStreamSynchronize(stream);  // nothing of this solve stays in flight
+    throw;
+  }
+  check(cudaStreamSynchronize(stream), "sync");
+}
+
+template <typename T>
+void PoolRunner::maxflow_epochs(T* res, T* exc, int* h, uint64_t* mask, const uint64_t* kmask,
+                                int* markv, SolveStats& stats, bool sets) {
   const int B = 256;
   k_pool_reset<<<nblk(n, B), B, 0, stream>>>(d_inst, n);
   count_launch();

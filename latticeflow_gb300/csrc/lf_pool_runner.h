@@ -187,6 +187,9 @@ class PoolRunner {
 
  private:
   template <typename T>
+  void maxflow_epochs(T* res, T* exc, int* h, uint64_t* mask, const uint64_t* kmask, int* mark,
+                      SolveStats& stats, bool sets);
+  template <typename T>
   void global_relabel(const T* res, const T* exc, int* h, uint64_t* mask, const uint64_t* kmask,
                       SolveStats& stats);
   template <typename T> unsigned long long activate(const T* exc, const int* h);
