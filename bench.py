@@ -429,6 +429,7 @@ def run_ours(args):
     }
     if rank == 0:
         out["cpu_baseline"] = cpu_baseline(p)
+        out["parity"] = parity_check(p, L)
         if not args.no_batch_summary and not args.profile_run:
             del L
             out["batched_vs_plain"] = batch_summary(args)
@@ -734,6 +735,18 @@ def cpu_baseline(p, budget_s=12.0):
     return {"value": round(len(times) / sum(times), 4), "unit": UNIT, "cores": 1, "kind": "port",
             "sample": "%d full solves of the same workload, reference push-relabel restated "
                       "(oracle/lf_oracle.cpp), median %.3f s" % (len(times), float(np.median(times)))}
+
+
+def parity_check(p, L):
+    """The timed workload's result against the oracle (the restated reference
+    solver on the same input): minimum energy, minimal and maximal on-sets."""
+    from oracle import oracle as O
+    O.build_port()
+    u, b = p.energies()
+    E, cmin, cmax, _, _ = O.port_canonical(p.kernel, p.dims, u, b)
+    energy = L.flow()[1]
+    ok = energy == E and np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
+    return bool(ok)
 
 
 # ---------------------------------------------------------------- reference

@@ -24,7 +24,7 @@ from . import kernels as _kernels
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "liblf_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_oracle.so")
-REF_SRC = "/root/reference/solver"
+REF_SRC = os.environ.get("LATTICEFLOW_REFERENCE_SOLVER", "/root/reference/solver")
 
 _SPECS = None
 _ALL_SPECS = None

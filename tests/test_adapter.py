@@ -6,7 +6,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/solver"
+REF = os.environ.get("LATTICEFLOW_REFERENCE_SOLVER", "/root/reference/solver")
 
 
 def test_adapter_compiles_against_reference_interface(native, tmp_path):

@@ -69,11 +69,23 @@ def test_names_validation(native):
 
 
 def test_no_cpu_fallback_in_package():
-    """The product package never imports the oracle."""
-    pkg = os.path.join(ROOT, "latticeflow_gb300")
-    for dirpath, _, files in os.walk(pkg):
-        for f in files:
-            if f.endswith(".py"):
-                txt = open(os.path.join(dirpath, f)).read()
-                assert "oracle" not in re.sub(r'""".*?"""', "", txt, flags=re.S).replace("oracle", "oracle", 0) or \
-                    "import oracle" not in txt and "from oracle" not in txt, f
+    """The product (package, native sources, C headers) never imports, loads
+    or links anything of the oracle: no Python import of it, and no path to
+    its libraries or sources in any product file, comments and docstrings
+    aside."""
+    roots = [os.path.join(ROOT, "latticeflow_gb300"), os.path.join(ROOT, "include")]
+    bad = re.compile(r"\boracle\b|liblf_oracle|libref_oracle|lf_oracle\.cpp|lfo_\w+\(")
+    for top in roots:
+        for dirpath, _, files in os.walk(top):
+            for f in files:
+                path = os.path.join(dirpath, f)
+                if f.endswith(".py"):
+                    txt = re.sub(r'"""(.|\n)*?"""', "", open(path).read())
+                    txt = "\n".join(l.split("#", 1)[0] for l in txt.splitlines())
+                elif f.endswith((".cu", ".cuh", ".cpp", ".h", ".hpp")):
+                    txt = re.sub(r"/\*(.|\n)*?\*/", "", open(path).read())
+                    txt = "\n".join(l.split("//", 1)[0] for l in txt.splitlines())
+                else:
+                    continue
+                m = bad.search(txt)
+                assert m is None, (path, m.group(0) if m else None)
