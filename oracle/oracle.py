@@ -79,6 +79,9 @@ def port():
         lib.lfo_pf_solve.argtypes = [ctypes.c_int, P, ctypes.c_int, P, P, P, P, P, P]
         lib.lfo_tv_single.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int, P, P, P,
                                       ctypes.c_double, P, P, P]
+        lib.lfo_tv_path.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int, P, P, P,
+                                    ctypes.c_int64, P, P, P, P]
+        lib.lfo_tv_path.restype = ctypes.c_int
         _port = lib
     return _port
 
@@ -204,6 +207,26 @@ def port_tv_single(kernel, f, lam):
                       _ptr(np.ascontiguousarray(w)), _ptr(f), float(lam), _ptr(out), _ptr(r),
                       ctypes.byref(t))
     return out, r, t.value
+
+
+def port_tv_path(kernel, f, lams):
+    """The reference's regularisation path restated (tv_solver.hpp:657-681):
+    (out[n_lambda][nx][ny], seconds, segments).  Raises ValueError when the
+    path tracker reports an error code."""
+    lib = port()
+    offs, w = lattice_offsets(kernel)
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    nx, ny = f.shape
+    lams = np.ascontiguousarray(lams, dtype=np.float64).reshape(-1)
+    out = np.zeros((len(lams), nx, ny), dtype=np.float64)
+    t = ctypes.c_double(0)
+    st = np.zeros(2, dtype=np.int64)
+    rc = lib.lfo_tv_path(nx, ny, len(offs), _ptr(np.ascontiguousarray(offs)),
+                         _ptr(np.ascontiguousarray(w)), _ptr(f), len(lams), _ptr(lams), _ptr(out),
+                         ctypes.byref(t), _ptr(st))
+    if rc != 0:
+        raise ValueError("port TV path failed: %d" % rc)
+    return out, t.value, int(st[0])
 
 
 def ref_solve(solver, kernel, dims, unary, binary):

@@ -7,8 +7,10 @@ Run where the reference sources are available (they are not on GPU hosts):
 Each cut case stores the integer energies (interface layout), the reference
 push-relabel labelling (LatticeEnergyMinimizer), the bundled BK labelling
 (BKGCEnergyMinimizer) and the minimum energy.  Each TV case stores the input
-image and calculate2dTV<Kernel, int64>'s output for one lambda.  The inputs
-are seeded, so the script is deterministic.
+image and calculate2dTV<Kernel, int64>'s output for one lambda; each path
+case the image, a list of lambdas and calculate2dTV's regularisation-path
+output (tv_solver.hpp:657-681).  The inputs are seeded, so the script is
+deterministic.
 """
 import os
 import sys
@@ -48,6 +50,30 @@ TV_CASES = [
     ("tv_f8_b", "Full2d_8", (24, 20), 30.0, 18),
     ("tv_s16_b", "Star2d_16", (16, 18), 20.0, 19),
 ]
+
+
+PATH_CASES = [
+    # name, kernel, image, lambdas (calculate2dTV(nx, ny, f, vector<double>))
+    ("f4_poly48", "Full2d_4", ("poly", 48, 6, 21), ("geom", 16)),
+    ("f8_poly40", "Full2d_8", ("poly", 40, 5, 22), ("geom", 12)),
+    ("s16_rand", "Star2d_16", ("rand", (24, 20), 23), ("list", [0.01, 0.05, 0.2, 1.0])),
+    ("f4_rand_unsorted", "Full2d_4", ("rand", (33, 30), 24), ("list", [0.3, -0.5, 0.01, 2.0, 0.07])),
+    ("f4_line", "Full2d_4", ("rand", (1, 40), 25), ("list", [0.1, 1.0])),
+    ("f4_poly64", "Full2d_4", ("poly", 64, 8, 26), ("geom", 64)),
+]
+
+
+def path_inputs(image, lams):
+    from latticeflow_gb300 import workloads as W
+    if image[0] == "poly":
+        f = W.tv_image(image[3], n=image[1], polygons=image[2])
+    else:
+        f = np.random.default_rng(image[2]).random(image[1])
+    if lams[0] == "geom":
+        lv = np.array([1e-3 * 1000.0 ** (i / (lams[1] - 1)) for i in range(lams[1])])
+    else:
+        lv = np.array(lams[1], dtype=np.float64)
+    return f, lv
 
 
 def make_energies(kernel, dims, gen, seed):
@@ -98,6 +124,14 @@ def main():
         np.savez_compressed(os.path.join(OUT, "tv_%s.npz" % name), kernel=kernel, f=f,
                             lam=np.float64(lam), out=out)
         print(name, float(out.min()), float(out.max()), len(np.unique(out)))
+    for name, kernel, image, lams in PATH_CASES:
+        f, lv = path_inputs(image, lams)
+        out, _ = O.ref_tv_path(kernel, f, lv)
+        again, _ = O.ref_tv_path(kernel, f, lv)
+        assert np.array_equal(out, again), name  # no event ties: the reference is repeatable
+        np.savez_compressed(os.path.join(OUT, "path_%s.npz" % name), kernel=kernel, f=f,
+                            lams=lv, out=out)
+        print(name, out.shape, float(out.min()), float(out.max()))
 
 
 if __name__ == "__main__":

@@ -218,6 +218,32 @@ def test_port_tv_against_compiled_reference(oracle_port):
         assert np.array_equal(ro, po)
 
 
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "path_*.npz"))),
+                         ids=lambda p: os.path.basename(p))
+def test_port_matches_reference_golden_path(oracle_port, path):
+    """The restated regularisation-path tracker reproduces the compiled
+    reference's calculate2dTV(nx, ny, f, lambdas) output bit for bit."""
+    O = oracle_port
+    z = np.load(path)
+    out, _, _ = O.port_tv_path(str(z["kernel"]), z["f"], z["lams"])
+    assert np.array_equal(out, z["out"])
+
+
+def test_port_path_against_compiled_reference(oracle_port):
+    O = oracle_port
+    if not O.ref_available():
+        pytest.skip("compiled reference not present")
+    from latticeflow_gb300 import workloads as W
+    rng = np.random.default_rng(31)
+    cases = [("Full2d_4", W.tv_image(3, n=56, polygons=6), [1e-3 * 1000 ** (i / 9) for i in range(10)]),
+             ("Full2d_8", rng.random((30, 26)), [0.02, 0.4, 0.0, 1.5]),
+             ("Star2d_16", W.tv_image(4, n=28, polygons=4), [0.05, 0.5])]
+    for kernel, f, lams in cases:
+        ro, _ = O.ref_tv_path(kernel, f, np.array(lams))
+        po, _, _ = O.port_tv_path(kernel, f, np.array(lams))
+        assert np.array_equal(ro, po), kernel
+
+
 def test_oracle_detects_planted_error(oracle_port):
     """A wrong labelling planted in the oracle's output is caught by the energy check."""
     O = oracle_port
