@@ -116,6 +116,10 @@ int lf_get_cut_max(const lf_lattice* h, int* cut_out);
 int lf_get_flow(const lf_lattice* h, int64_t* flow, int64_t* energy);
 /* Parametric solver: final 2x-scaled node values r (pf_flow_node.hpp:233-235). */
 int lf_get_levels(const lf_lattice* h, int64_t* r_out);
+/* Parametric solver: the level set of every node (int[N], row-major), the
+ * level sets numbered in the order ParametricFlowSolver::run returns them
+ * (parametricflow/pf_solver.hpp:180-203). */
+int lf_get_level_sets(const lf_lattice* h, int32_t* sets_out);
 /* Statistics of the last run: epochs (global relabels), push-relabel
  * launches, BFS passes.  Any pointer may be NULL. */
 int lf_get_stats(const lf_lattice* h, int64_t* epochs, int64_t* pr_launches,
@@ -256,18 +260,28 @@ int lf_cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* s
  * levels_out (may be NULL): the final 2x-scaled fixed-point values r. */
 int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double lambda,
              double* out, int64_t* levels_out);
+/* The same, also giving the level set of every pixel (sets_out: nx*ny
+ * int32, may be NULL), numbered in the order the reference's parametric
+ * solver returns them (parametricflow/pf_solver.hpp:180-203). */
+int lf_tv_2d_level_sets(const char* kernel, size_t nx, size_t ny, const double* f,
+                        double lambda, double* out, int64_t* levels_out, int32_t* sets_out);
 
 /* calculate2dTV<Kernel, int64>(nx, ny, f, vector<double> lambdas)
- * (tv/tv_solver.hpp:657-681): the denoised image at every lambda,
- * out[n_lambda][nx][ny].  Slice i is the single-lambda solution at
- * lambdas[i] (what lf_tv_2d returns), all lambdas solved together as
- * lf_tv_2d_batch solves them.  The
- * reference traces the path instead with piecewise-linear region segments
- * (tv/tv_regpath_node.hpp), whose values differ from its own single-lambda
- * solutions away from the smallest lambdas.  As in the reference a negative
+ * (tv/tv_solver.hpp:657-681): the reference's regularisation path,
+ * out[n_lambda][nx][ny].  Solved once at the largest lambda, then tracked
+ * downwards with the reference's event heap of region segments (joins,
+ * splits found by region max-flow probes and integer bisection,
+ * tv/tv_regpath_node.hpp), the probes and all lattice work on the GPU; the
+ * output is each pixel's segment line at every lambda, as the reference
+ * traces it (these values are not the single-lambda solutions: for those,
+ * call lf_tv_2d_batch with f_stride = 0).  As in the reference a negative
  * lambda counts as 0 and n_lambda = 0 returns at once. */
 int lf_tv_2d_path(const char* kernel, size_t nx, size_t ny, const double* f, size_t n_lambda,
                   const double* lambdas, double* out);
+/* The same, with statistics (stats: 4 int64, may be NULL): path segments,
+ * region probes (device max-flows), events applied, initial level sets. */
+int lf_tv_2d_path_stats(const char* kernel, size_t nx, size_t ny, const double* f,
+                        size_t n_lambda, const double* lambdas, double* out, int64_t* stats);
 
 /* Many single-lambda TV problems of one shape solved together on the GPU:
  * problem p is the image at f + p * f_stride (f_stride = 0: one image for

@@ -37,6 +37,7 @@ PROTOTYPES = {
     "lf_get_cut_max": (I, [P, P]),
     "lf_get_flow": (I, [P, P, P]),
     "lf_get_levels": (I, [P, P]),
+    "lf_get_level_sets": (I, [P, P]),
     "lf_get_stats": (I, [P, P, P, P]),
     "lf_set_tuning": (I, [P, I, I, I]),
     "lf_set_param": (I, [P, ctypes.c_char_p, I]),
@@ -46,7 +47,9 @@ PROTOTYPES = {
     "lf_get_stream": (I, [P, P]),
     "lf_get_layout": (I, [P, P, P, P]),
     "lf_tv_2d": (I, [ctypes.c_char_p, SZ, SZ, P, ctypes.c_double, P, P]),
+    "lf_tv_2d_level_sets": (I, [ctypes.c_char_p, SZ, SZ, P, ctypes.c_double, P, P, P]),
     "lf_tv_2d_path": (I, [ctypes.c_char_p, SZ, SZ, P, SZ, P, P]),
+    "lf_tv_2d_path_stats": (I, [ctypes.c_char_p, SZ, SZ, P, SZ, P, P, P]),
     "lf_tv_2d_batch": (I, [ctypes.c_char_p, SZ, SZ, SZ, P, SZ, P, P, P, SZ]),
     "lf_batch_create": (I, [P]),
     "lf_batch_destroy": (None, [P]),

@@ -213,6 +213,16 @@ int lf_get_levels(const lf_lattice* h, int64_t* out) {
   });
 }
 
+int lf_get_level_sets(const lf_lattice* h, int32_t* out) {
+  return guarded([&] {
+    if (!h || !out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    const lfg::Engine& e = *h->e;
+    if (!e.solved || !e.parametric)
+      throw lfg::LfError{LF_ERR_STATE, "level sets are available after a parametric run"};
+    std::memcpy(out, e.level_sets_host.data(), e.N * sizeof(int32_t));
+  });
+}
+
 int lf_get_stats(const lf_lattice* h, int64_t* epochs, int64_t* pr, int64_t* bfs) {
   if (!h) return LF_ERR_INVALID;
   if (epochs) *epochs = h->e->stats.epochs;
@@ -298,28 +308,35 @@ const lfg::KernelDef* tv_kernel(const char* kernel) {
 }
 }  // namespace
 
-int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double lambda,
-             double* out, int64_t* levels_out) {
+int lf_tv_2d_level_sets(const char* kernel, size_t nx, size_t ny, const double* f,
+                        double lambda, double* out, int64_t* levels_out, int32_t* sets_out) {
   return guarded([&] {
     const lfg::KernelDef* k = tv_kernel(kernel);
     if (!f || !out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
-    int rc = lfg::tv_2d(k, nx, ny, f, lambda, out, levels_out);
+    int rc = lfg::tv_2d(k, nx, ny, f, lambda, out, levels_out, sets_out);
     if (rc) throw lfg::LfError{rc, "tv solve failed"};
+  });
+}
+
+int lf_tv_2d(const char* kernel, size_t nx, size_t ny, const double* f, double lambda,
+             double* out, int64_t* levels_out) {
+  return lf_tv_2d_level_sets(kernel, nx, ny, f, lambda, out, levels_out, nullptr);
+}
+
+int lf_tv_2d_path_stats(const char* kernel, size_t nx, size_t ny, const double* f,
+                        size_t n_lambda, const double* lambdas, double* out, int64_t* stats) {
+  return guarded([&] {
+    const lfg::KernelDef* k = tv_kernel(kernel);
+    if (n_lambda == 0 || nx * ny == 0) return;
+    if (!f || !out || !lambdas) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    int rc = lfg::tv_2d_path(k, nx, ny, f, n_lambda, lambdas, out, stats);
+    if (rc) throw lfg::LfError{rc, "tv path failed"};
   });
 }
 
 int lf_tv_2d_path(const char* kernel, size_t nx, size_t ny, const double* f, size_t n_lambda,
                   const double* lambdas, double* out) {
-  return guarded([&] {
-    const lfg::KernelDef* k = tv_kernel(kernel);
-    if (n_lambda == 0 || nx * ny == 0) return;
-    if (!f || !out || !lambdas) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
-    std::vector<double> lam(lambdas, lambdas + n_lambda);
-    for (double& l : lam)
-      if (!(l >= 0)) l = 0;  // tv_solver.hpp:669-674
-    int rc = lfg::tv_2d_batch(k, nx, ny, n_lambda, f, 0, lam.data(), out, nullptr, 0);
-    if (rc) throw lfg::LfError{rc, "tv path failed"};
-  });
+  return lf_tv_2d_path_stats(kernel, nx, ny, f, n_lambda, lambdas, out, nullptr);
 }
 
 int lf_tv_2d_batch(const char* kernel, size_t nx, size_t ny, size_t count, const double* f,

@@ -120,6 +120,9 @@ class Engine : public ProfHooks {
   cudaError_t counted(cudaError_t e) { ++launches; return e; }
   int* d_cuts = nullptr;  // [2N] minimal / maximal on-set, filled by extract_cuts
   std::vector<int64_t> levels_host;
+  // parametric solver: level set of every node (row-major), numbered in the
+  // order the reference returns its level sets (pf_solver.hpp:180-203)
+  std::vector<int> level_sets_host;
 
   void choose_geometry(int elem);
   void alloc_accumulators();
@@ -138,7 +141,13 @@ int cut_2d_noalloc(const char* kernel, size_t nx, size_t ny, const int32_t* src,
                    const int32_t* snk, const int32_t* edge, int32_t* cut, int64_t* flow_energy,
                    cudaStream_t s);  // lf_noalloc.cu
 int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lambda, double* out,
-          int64_t* levels_out);
+          int64_t* levels_out, int32_t* sets_out = nullptr);
+void tv_fill_single(Engine& E, const double* f, double lambda, double* mean, double* scale,
+                    std::vector<int64_t>* base_fv, std::vector<long long>* pwf2_out);
+// the reference's regularisation path (lf_tvpath.cu); stats (may be null):
+// [0] path segments, [1] region probes, [2] events, [3] initial level sets
+int tv_2d_path(const KernelDef* kd, size_t nx, size_t ny, const double* f, size_t n_lambda,
+               const double* lambdas, double* out, int64_t* stats);
 int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* levels_out);
 int tv_2d_stack_on(Engine& E, size_t nx, size_t ny, size_t count, const double* f,
                    size_t f_stride, const double* lambdas, double* out, int64_t* levels_out);

@@ -147,10 +147,12 @@ __global__ void k_pf_stats(long long NP, const int* key, const long long* exc,
 }
 
 // Sections marked finished fold their offset into the node (offset 0, as the
-// reference's final setOffset(0)) and leave the computation (key -2); the
-// others move their offset: exc += off_new - off_old.
+// reference's final setOffset(0)) and leave the computation (key -2),
+// recording the level set they end in (leaf[s]); the others move their
+// offset: exc += off_new - off_old.
 __global__ void k_pf_apply(long long NP, int* key, long long* exc, const long long* off_old,
-                           const long long* off_new, const unsigned char* finished) {
+                           const long long* off_new, const unsigned char* finished,
+                           const int* leaf, int* lset) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= NP) return;
   int s = key[i];
@@ -158,6 +160,7 @@ __global__ void k_pf_apply(long long NP, int* key, long long* exc, const long lo
   if (finished[s]) {
     exc[i] -= off_old[s];
     key[i] = -2;
+    lset[i] = leaf[s];
   } else {
     exc[i] += off_new[s] - off_old[s];
   }
@@ -200,12 +203,15 @@ __global__ void k_pf_remap(long long NP, int* key, const int* h, const int* chil
   key[i] = child[2 * s + side];
 }
 
-__global__ void k_pf_levels(Geo g, int nd, long long N, const long long* exc, int64_t* r) {
+__global__ void k_pf_levels(Geo g, int nd, long long N, const long long* exc, const int* lset,
+                            int64_t* r, int* ls) {
   long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= N) return;
   int a, bb, c;
   bounded_coords(g, nd, b, a, bb, c);
-  r[b] = -exc[((long long)a * g.Bp + bb) * g.Cp + c];
+  const long long i = ((long long)a * g.Bp + bb) * g.Cp + c;
+  r[b] = -exc[i];
+  ls[b] = lset[i];
 }
 
 }  // namespace
@@ -256,7 +262,7 @@ void engine_run_parametric(Engine& E) {
   DevBuf<long long> off_old, off_new, rmin, rmax;
   DevBuf<unsigned long long> lo, hi, cnt, cnt2;
   DevBuf<unsigned char> fin;
-  DevBuf<int> child;
+  DevBuf<int> child, leaf, lset;
   key.alloc(NP, s);
   off_old.alloc(cap_sections, s);
   off_new.alloc(cap_sections, s);
@@ -268,6 +274,8 @@ void engine_run_parametric(Engine& E) {
   cnt2.alloc(2 * cap_sections, s);
   fin.alloc(cap_sections, s);
   child.alloc(2 * cap_sections, s);
+  leaf.alloc(cap_sections, s);
+  lset.alloc(NP, s);
   if (!E.d_kmask) E.check(cudaMalloc(&E.d_kmask, NP * sizeof(uint64_t)), "cudaMalloc kmask");
   // (the section mask stays allocated with the engine for its next solve)
 
@@ -280,7 +288,14 @@ void engine_run_parametric(Engine& E) {
   std::vector<unsigned long long> h_lo, h_hi, h_cnt, h_cnt2;
   std::vector<long long> h_min, h_max, h_off, h_new;
   std::vector<unsigned char> h_fin;
-  std::vector<int> h_child;
+  std::vector<int> h_child, h_leaf;
+  // Level sets in the reference's order: the reference partitions one node
+  // list in place, the lower (off) part of a range before its upper (on)
+  // part, and returns the final ranges by position (pf_solver.hpp:101-203).
+  // pos[s] = first position of section s in that list; a finished section
+  // is a level set (leaf), ordered by its position.
+  std::vector<long long> pos(S, 0), leaf_pos;
+  for (long long p = 0; p < S; ++p) pos[p] = p * (long long)real * std::max(E.g.C, 1);
   const long long max_rounds = 20000;
   const bool trace = std::getenv("LF_PF_TRACE") != nullptr;  // diagnostic: one line per generation
   for (long long round = 0; S > 0; ++round) {
@@ -307,8 +322,15 @@ void engine_run_parametric(Engine& E) {
     E.check(cudaStreamSynchronize(s), "sync");
     // 2. the reference's offset rule, exactly (pf_flow_node.hpp:364-374)
     long long solving = 0;
+    h_leaf.assign(S, -1);
     for (long long i = 0; i < S; ++i) {
-      if (h_max[i] - h_min[i] <= 1) { h_fin[i] = 1; h_new[i] = h_off[i]; continue; }
+      if (h_max[i] - h_min[i] <= 1) {
+        h_fin[i] = 1;
+        h_new[i] = h_off[i];
+        h_leaf[i] = int(leaf_pos.size());
+        leaf_pos.push_back(pos[i]);
+        continue;
+      }
       __int128 sum = (__int128)(((unsigned __int128)h_hi[i] << 64) | h_lo[i]);
       double count = double(h_cnt[i]);
       long long r_new = (long long)std::ceil(double(sum) / count);
@@ -324,7 +346,10 @@ void engine_run_parametric(Engine& E) {
     }
     E.check(cudaMemcpyAsync(off_new.p, h_new.data(), S * 8, cudaMemcpyHostToDevice, s), "memcpy");
     E.check(cudaMemcpyAsync(fin.p, h_fin.data(), S, cudaMemcpyHostToDevice, s), "memcpy");
-    k_pf_apply<<<nblk(NP, 256), 256, 0, s>>>(NP, key.p, exc, off_old.p, off_new.p, fin.p);
+    E.check(cudaMemcpyAsync(leaf.p, h_leaf.data(), S * sizeof(int), cudaMemcpyHostToDevice, s),
+            "memcpy");
+    k_pf_apply<<<nblk(NP, 256), 256, 0, s>>>(NP, key.p, exc, off_old.p, off_new.p, fin.p, leaf.p,
+                                             lset.p);
     E.check(E.counted(cudaGetLastError()), "pf apply");
     if (solving == 0) { E.check(cudaStreamSynchronize(s), "sync"); break; }
     // 3. one max-flow for every solving section
@@ -339,7 +364,7 @@ void engine_run_parametric(Engine& E) {
     E.check(cudaMemcpyAsync(h_cnt2.data(), cnt2.p, 2 * S * 8, cudaMemcpyDeviceToHost, s), "memcpy");
     E.check(cudaStreamSynchronize(s), "sync");
     h_child.assign(2 * S, -1);
-    std::vector<long long> next_off;
+    std::vector<long long> next_off, next_pos;
     long long S2 = 0;
     for (long long i = 0; i < S; ++i) {
       if (h_fin[i]) continue;
@@ -347,8 +372,10 @@ void engine_run_parametric(Engine& E) {
         if (h_cnt2[2 * i + side] > 0) {
           h_child[2 * i + side] = int(S2++);
           next_off.push_back(h_new[i]);
+          next_pos.push_back(pos[i] + (side ? (long long)h_cnt2[2 * i] : 0));
         }
     }
+    pos.swap(next_pos);
     if (S2 > cap_sections) throw LfError{4, "section count overflow"};
     E.check(cudaMemcpyAsync(child.p, h_child.data(), 2 * S * sizeof(int), cudaMemcpyHostToDevice, s), "memcpy");
     k_pf_remap<<<nblk(NP, 256), 256, 0, s>>>(NP, key.p, E.d_h, child.p);
@@ -366,13 +393,25 @@ void engine_run_parametric(Engine& E) {
   }
   E.check(cudaEventRecord(E.ev1, s), "event");
   E.levels_host.assign((size_t)E.N, 0);
+  E.level_sets_host.assign((size_t)E.N, 0);
   if (E.N > 0) {
     DevBuf<int64_t> r;
+    DevBuf<int> ls;
     r.alloc(E.N, s);
-    k_pf_levels<<<nblk(E.N, 256), 256, 0, s>>>(g, E.nd, E.N, exc, r.p);
+    ls.alloc(E.N, s);
+    k_pf_levels<<<nblk(E.N, 256), 256, 0, s>>>(g, E.nd, E.N, exc, lset.p, r.p, ls.p);
     E.check(E.counted(cudaGetLastError()), "pf levels");
     E.check(cudaMemcpyAsync(E.levels_host.data(), r.p, E.N * 8, cudaMemcpyDeviceToHost, s), "memcpy");
+    E.check(cudaMemcpyAsync(E.level_sets_host.data(), ls.p, E.N * sizeof(int),
+                            cudaMemcpyDeviceToHost, s), "memcpy");
     E.check(cudaStreamSynchronize(s), "sync");
+    // leaf ids -> level-set index in the reference's order (by position)
+    std::vector<int> order(leaf_pos.size()), rank(leaf_pos.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = int(i);
+    std::sort(order.begin(), order.end(),
+              [&](int a, int b) { return leaf_pos[a] < leaf_pos[b]; });
+    for (size_t i = 0; i < order.size(); ++i) rank[order[i]] = int(i);
+    for (int& v : E.level_sets_host) v = v >= 0 && size_t(v) < rank.size() ? rank[v] : -1;
   }
   float ms = 0;
   cudaEventElapsedTime(&ms, E.ev0, E.ev1);
@@ -485,6 +524,41 @@ int tv_2d_stack_on(Engine& E, size_t nx, size_t ny, size_t count, const double* 
   return 0;
 }
 
+// TV setup of one image on a single-problem parametric engine of shape
+// (nx, ny) (tv/tv_solver.hpp:71-112, max_lambda = lambda): fills the
+// engine's accumulators, returns the image mean and scale and, per node in
+// row-major order, the base value 2 uf (PFFlowNode::base_fv after
+// pullBaseFunctionValueFromLattice, pf_flow_node.hpp:398-406).
+void tv_fill_single(Engine& E, const double* f, double lambda, double* mean, double* scale,
+                    std::vector<int64_t>* base_fv, std::vector<long long>* pwf2_out) {
+  const KernelDef* kd = E.kd;
+  const size_t nx = E.dims[0], ny = E.dims[1], N = nx * ny;
+  if (E.nd != 2 || E.sub_count > 1) throw LfError{2, "TV fill takes one 2-d lattice"};
+  TVImage t = tv_setup(f, N);
+  std::vector<long long> pwf2(kd->K);
+  tv_edges(kd, t.scale, lambda, pwf2.data());
+  E.alloc_accumulators();
+  DevBuf<int64_t> d_uf;
+  DevBuf<long long> d_pwf;
+  d_uf.alloc(N, E.stream);
+  d_pwf.alloc(pwf2.size(), E.stream);
+  E.check(cudaMemcpyAsync(d_uf.p, t.uf.data(), N * 8, cudaMemcpyHostToDevice, E.stream), "memcpy");
+  E.check(cudaMemcpyAsync(d_pwf.p, pwf2.data(), pwf2.size() * 8, cudaMemcpyHostToDevice,
+                          E.stream), "memcpy");
+  k_fill_tv<<<nblk((long long)N, 256), 256, 0, E.stream>>>(E.g, E.st, (long long)N, int(nx),
+                                                           int(nx), 0LL, d_uf.p, d_pwf.p,
+                                                           E.d_exc64, E.d_cap64);
+  E.check(cudaGetLastError(), "fill tv");
+  E.check(cudaStreamSynchronize(E.stream), "sync");
+  *mean = t.mean;
+  *scale = t.scale;
+  if (base_fv) {
+    base_fv->resize(N);
+    for (size_t i = 0; i < N; ++i) (*base_fv)[i] = 2 * t.uf[i];
+  }
+  if (pwf2_out) *pwf2_out = pwf2;
+}
+
 // calculate2dTV<Kernel, int64>(nx, ny, f, lambda)  (tv/tv_solver.hpp:650-655)
 // on an existing parametric engine of shape (nx, ny) (its buffers are reused).
 int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* levels_out) {
@@ -492,11 +566,14 @@ int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* le
 }
 
 int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lambda, double* out,
-          int64_t* levels_out) {
+          int64_t* levels_out, int32_t* sets_out) {
   if (nx * ny == 0) return 0;
   size_t dims[2] = {nx, ny};
   Engine E("GPULevelReductions", kd, 2, dims);
-  return tv_2d_on(E, f, lambda, out, levels_out);
+  const int rc = tv_2d_on(E, f, lambda, out, levels_out);
+  if (sets_out)
+    std::memcpy(sets_out, E.level_sets_host.data(), nx * ny * sizeof(int32_t));
+  return rc;
 }
 
 Engine* new_tv_stack_engine(const KernelDef* kd, size_t nx, size_t ny, size_t count) {

@@ -267,34 +267,57 @@ class LatticeFlow(object):
         N.check(N.lib().lf_get_levels(self._h, _p(out)))
         return out.reshape(self._dimensions)
 
+    def levelSets(self):
+        """Parametric solver: the level set of every node, numbered in the
+        order ParametricFlowSolver::run returns the level sets
+        (parametricflow/pf_solver.hpp:180-203)."""
+        out = np.empty(self.n_nodes, dtype=np.int32)
+        N.check(N.lib().lf_get_level_sets(self._h, _p(out)))
+        return out.reshape(self._dimensions)
+
     def stats(self):
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         N.check(N.lib().lf_get_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return {"epochs": a.value, "pr_launches": b.value, "bfs_passes": c.value}
 
 
-def calculate2dTV(f, lam, kernel="Full2d_4", return_levels=False):
-    """Single-lambda TV (tv/tv_solver.hpp:650-655) on the GPU."""
+def calculate2dTV(f, lam, kernel="Full2d_4", return_levels=False, return_sets=False):
+    """Single-lambda TV (tv/tv_solver.hpp:650-655) on the GPU.
+
+    return_levels: also the final 2x-scaled values r; return_sets: also the
+    level set of every pixel, numbered in the reference solver's order."""
     f = np.ascontiguousarray(f, dtype=np.float64)
     if f.ndim != 2:
         raise ValueError("calculate2dTV takes a 2-d array")
     nx, ny = f.shape
     out = np.empty((nx, ny), dtype=np.float64)
     lv = np.empty((nx, ny), dtype=np.int64)
-    N.check(N.lib().lf_tv_2d(kernel.encode(), nx, ny, _p(f), float(lam), _p(out), _p(lv)))
-    return (out, lv) if return_levels else out
+    sets = np.empty((nx, ny), dtype=np.int32)
+    N.check(N.lib().lf_tv_2d_level_sets(kernel.encode(), nx, ny, _p(f), float(lam), _p(out),
+                                        _p(lv), _p(sets)))
+    res = (out,)
+    if return_levels:
+        res += (lv,)
+    if return_sets:
+        res += (sets,)
+    return res if len(res) > 1 else out
 
 
-def calculate2dTVPath(f, lambdas, kernel="Full2d_4"):
-    """TV at every lambda (calculate2dTV with a lambda list,
+def calculate2dTVPath(f, lambdas, kernel="Full2d_4", return_stats=False):
+    """The regularisation path (calculate2dTV with a lambda list,
     tv/tv_solver.hpp:657-681) -> array [len(lambdas), nx, ny].
 
-    Slice i is the single-lambda solution at lambdas[i] (equal to
-    ``calculate2dTV(f, lambdas[i])``); all lambdas are solved together on the
-    GPU.  Negative lambdas count as 0, as in the reference.  (The Cython
-    wrappers also rescale their output, ``pylatticeflow.pyx:452`` by lambda
-    and ``:482`` by a stale lambda; these functions return the C++ entries'
-    values unscaled.)
+    The reference's path tracker: one parametric solve at the largest
+    lambda, then region segments followed down in lambda (joins, and splits
+    found by region max-flow probes on the GPU); slice i is every pixel's
+    segment line at lambdas[i], as the reference traces it.  These values
+    are not the single-lambda solutions; for those use
+    ``calculate2dTVBatch(f, lambdas)``.  Negative lambdas count as 0, as in
+    the reference.  (The Cython wrappers also rescale their output,
+    ``pylatticeflow.pyx:452`` by lambda and ``:482`` by a stale lambda;
+    these functions return the C++ entries' values unscaled.)
+
+    return_stats: also return {"segments", "probes", "events", "level_sets"}.
     """
     f = np.ascontiguousarray(f, dtype=np.float64)
     if f.ndim != 2:
@@ -304,7 +327,12 @@ def calculate2dTVPath(f, lambdas, kernel="Full2d_4"):
         raise ValueError("lambdas must be a 1-d sequence")
     nx, ny = f.shape
     out = np.empty((lam.size, nx, ny), dtype=np.float64)
-    N.check(N.lib().lf_tv_2d_path(kernel.encode(), nx, ny, _p(f), lam.size, _p(lam), _p(out)))
+    st = np.zeros(4, dtype=np.int64)
+    N.check(N.lib().lf_tv_2d_path_stats(kernel.encode(), nx, ny, _p(f), lam.size, _p(lam),
+                                        _p(out), _p(st)))
+    if return_stats:
+        return out, {"segments": int(st[0]), "probes": int(st[1]), "events": int(st[2]),
+                     "level_sets": int(st[3])}
     return out
 
 
@@ -417,6 +445,14 @@ class LatticeBatch(object):
         e = ctypes.c_int64(0)
         N.check(N.lib().lf_batch_get_flow(self._h, index, ctypes.byref(f), ctypes.byref(e)))
         return f.value, e.value
+
+    def levelSets(self):
+        """Parametric solver: the level set of every node, numbered in the
+        order ParametricFlowSolver::run returns the level sets
+        (parametricflow/pf_solver.hpp:180-203)."""
+        out = np.empty(self.n_nodes, dtype=np.int32)
+        N.check(N.lib().lf_get_level_sets(self._h, _p(out)))
+        return out.reshape(self._dimensions)
 
     def stats(self):
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

@@ -1307,15 +1307,24 @@ int lfo_pr_canonical(int nd, const int64_t* dims, int K, const int* offsets,
 
 // Parametric flow over the filled lattice (LatticeLevelReductions).  r_out[N]
 // receives the final 2x-scaled reductions, cut_out[N] = (reduction < 0)
-// (network_flow_node.hpp:50-55 with on_by_reduction).
+// (network_flow_node.hpp:50-55 with on_by_reduction), sets_out[N] (may be
+// NULL) the index of every node's level set in the order run() returns them.
 int lfo_pf_solve(int nd, const int64_t* dims, int K, const int* offsets,
                  const int64_t* unary, const int64_t* binary, int64_t* r_out,
-                 int32_t* cut_out, double* seconds) {
+                 int32_t* cut_out, double* seconds, int32_t* sets_out) {
   Problem P;
   P.init(nd, dims, K, offsets);
   P.fill(unary, binary);
   auto t0 = std::chrono::steady_clock::now();
-  run_pf(P);
+  std::vector<std::vector<int64_t>> level_sets;
+  run_pf(P, &level_sets);
+  if (sets_out) {
+    std::vector<int32_t> id(size_t(P.L.size_all), -1);
+    for (size_t i = 0; i < level_sets.size(); ++i)
+      for (int64_t p : level_sets[i]) id[size_t(p)] = int32_t(i);
+    const int64_t N = P.L.n_bounded();
+    for (int64_t b = 0; b < N; ++b) sets_out[b] = id[size_t(P.L.padded(b))];
+  }
   auto t1 = std::chrono::steady_clock::now();
   if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
   int64_t N = P.L.n_bounded();
@@ -1328,9 +1337,11 @@ int lfo_pf_solve(int nd, const int64_t* dims, int K, const int* offsets,
 }
 
 // TVSolver<Kernel, int64>::runSingleLambda (tv_solver.hpp:71-112,151-176).
-// weights: geocut weights in lattice order.  out[N] doubles, r_out[N] raw r().
+// weights: geocut weights in lattice order.  out[N] doubles, r_out[N] raw r(),
+// sets_out[N] (may be NULL) the level set of every node (run()'s order).
 int lfo_tv_single(int64_t nx, int64_t ny, int K, const int* offsets, const double* weights,
-                  const double* f, double lam, double* out, int64_t* r_out, double* seconds) {
+                  const double* f, double lam, double* out, int64_t* r_out, double* seconds,
+                  int32_t* sets_out) {
   const int nbits = 40;  // n_bits_function_precision for int64 (pf_flow_node.hpp:111-113)
   const double fscale = double(int64_t(1) << nbits);
   Problem P;
@@ -1364,7 +1375,14 @@ int lfo_tv_single(int64_t nx, int64_t ny, int K, const int* offsets, const doubl
       P.addE2(p, e, 0, pwf, pwf, 0);
     }
   }
-  run_pf(P);
+  std::vector<std::vector<int64_t>> level_sets;
+  run_pf(P, &level_sets);
+  if (sets_out) {
+    std::vector<int32_t> id(size_t(P.L.size_all), -1);
+    for (size_t i = 0; i < level_sets.size(); ++i)
+      for (int64_t p : level_sets[i]) id[size_t(p)] = int32_t(i);
+    for (int64_t b = 0; b < N; ++b) sets_out[b] = id[size_t(P.L.padded(b))];
+  }
   double sum = 0;
   std::vector<double> R(static_cast<size_t>(N));
   for (int64_t b = 0; b < N; ++b) {

@@ -76,9 +76,9 @@ def port():
         P = ctypes.c_void_p
         lib.lfo_pr_solve.argtypes = [ctypes.c_int, P, ctypes.c_int, P, P, P, P, P]
         lib.lfo_pr_canonical.argtypes = [ctypes.c_int, P, ctypes.c_int, P, P, P, P, P, P, P]
-        lib.lfo_pf_solve.argtypes = [ctypes.c_int, P, ctypes.c_int, P, P, P, P, P, P]
+        lib.lfo_pf_solve.argtypes = [ctypes.c_int, P, ctypes.c_int, P, P, P, P, P, P, P]
         lib.lfo_tv_single.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int, P, P, P,
-                                      ctypes.c_double, P, P, P]
+                                      ctypes.c_double, P, P, P, P]
         lib.lfo_tv_path.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int, P, P, P,
                                     ctypes.c_int64, P, P, P, P]
         lib.lfo_tv_path.restype = ctypes.c_int
@@ -180,7 +180,9 @@ def port_canonical(kernel, dims, unary, binary):
     return E, cmin.reshape(dims), cmax.reshape(dims), cpr.reshape(dims), t.value
 
 
-def port_pf(kernel, dims, unary, binary):
+def port_pf(kernel, dims, unary, binary, return_sets=False):
+    """Restated parametric flow: (final r, reduction < 0 cut, seconds) and,
+    with return_sets, the level set of every node in the reference's order."""
     lib = port()
     offs, _ = lattice_offsets(kernel)
     d = np.asarray(dims, dtype=np.int64)
@@ -189,23 +191,31 @@ def port_pf(kernel, dims, unary, binary):
     N = int(np.prod(dims))
     r = np.zeros(N, dtype=np.int64)
     cut = np.zeros(N, dtype=np.int32)
+    sets = np.zeros(N, dtype=np.int32)
     t = ctypes.c_double(0)
     lib.lfo_pf_solve(len(dims), _ptr(d), len(offs), _ptr(np.ascontiguousarray(offs)),
-                     _ptr(u), _ptr(b), _ptr(r), _ptr(cut), ctypes.byref(t))
+                     _ptr(u), _ptr(b), _ptr(r), _ptr(cut), ctypes.byref(t), _ptr(sets))
+    if return_sets:
+        return r.reshape(dims), cut.reshape(dims), t.value, sets.reshape(dims)
     return r.reshape(dims), cut.reshape(dims), t.value
 
 
-def port_tv_single(kernel, f, lam):
+def port_tv_single(kernel, f, lam, return_sets=False):
+    """Restated single-lambda TV: (out, raw r, seconds) and, with
+    return_sets, the level set of every node in the reference's order."""
     lib = port()
     offs, w = lattice_offsets(kernel)
     f = np.ascontiguousarray(f, dtype=np.float64)
     nx, ny = f.shape
     out = np.zeros((nx, ny), dtype=np.float64)
     r = np.zeros((nx, ny), dtype=np.int64)
+    sets = np.zeros((nx, ny), dtype=np.int32)
     t = ctypes.c_double(0)
     lib.lfo_tv_single(nx, ny, len(offs), _ptr(np.ascontiguousarray(offs)),
                       _ptr(np.ascontiguousarray(w)), _ptr(f), float(lam), _ptr(out), _ptr(r),
-                      ctypes.byref(t))
+                      ctypes.byref(t), _ptr(sets))
+    if return_sets:
+        return out, r, t.value, sets
     return out, r, t.value
 
 

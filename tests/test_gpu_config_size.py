@@ -11,8 +11,8 @@ seeded input at full size:
 * the 512-lattice batch of uneven 4- and 8-connected cuts, lattice by
   lattice: the same;
 * one single-lambda TV solve of the 1024 x 1024 polygon image: levels
-  within one raw unit (2^-41 of the function range), the lattice total
-  exact, doubles within 1e-9 relative.
+  the level-set partition and every level set's total exact, levels within
+  one raw unit (2^-41 of the function range), doubles within 1e-9 relative.
 """
 import numpy as np
 import pytest
@@ -79,10 +79,11 @@ def test_batch_512_vs_oracle(native, gpu, oracle_port):
 def test_tv_single_1024_vs_oracle(native, gpu, oracle_port):
     import latticeflow_gb300 as lf
     from latticeflow_gb300 import workloads as W
+    from test_gpu_param import check_level_sets
     f = W.tv_image(0)
     lam = 0.05
-    out, lv = lf.calculate2dTV(f, lam, return_levels=True)
-    ref, r, _ = oracle_port.port_tv_single("Full2d_4", f, lam)
-    assert int(np.abs(lv - r).max()) <= 1
+    out, lv, sets = lf.calculate2dTV(f, lam, return_levels=True, return_sets=True)
+    ref, r, _, sets_ref = oracle_port.port_tv_single("Full2d_4", f, lam, return_sets=True)
+    check_level_sets(lv, sets, r, sets_ref)
     assert int(lv.sum()) == int(r.sum())
     assert float(np.abs(out - ref).max()) <= 1e-9 * max(1.0, float(np.abs(ref).max()))
