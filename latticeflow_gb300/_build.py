@@ -17,7 +17,11 @@ LIB = os.path.join(LIBDIR, "liblatticeflow_gpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
+# -ffp-contract=off: host double arithmetic (TV set-up and output) rounds
+# every operation as written, as the reference's x86 build does; an Arm
+# host compiler would otherwise fuse multiply-adds
+FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
+         "-ffp-contract=off", "-I" + INCLUDE]
 
 
 def nvcc():
