@@ -225,6 +225,229 @@ __global__ void k_seg_probe(const int* nodes, int n, int key, const int* keys, c
   if ((threadIdx.x & 31) == 0 && ons) atomicAdd(cnt, (unsigned long long)ons);
 }
 
+// ------------------------------------------------ fused small-region probe
+//
+// setRegionToLambda and runPartitionedSection of one region of at most
+// kSmallRegion nodes in ONE block: the region's influence sum, the offset
+// (floorAverage of a 128-bit sum), every node's new offset and scale, a
+// push/relabel max-flow on the region alone (exact BFS relabels from the
+// deficits, synchronous pushes along admissible edges, local relabels
+// between them), and the probe's read-out -- labels of the maximal on-set
+// (nodes that cannot reach a deficit), the per-side influence sums and the
+// cut value -- with no host round trip in between.  Residuals stay in the
+// lattice arrays (a small region is cache resident); excess, heights and the
+// region's local neighbour table live in shared memory.
+constexpr int kSmallRegion = 2048;
+constexpr int kHUnreached = 0x3fffffff;
+
+// truncating 128-bit / positive 32-bit division by 32-bit limbs
+__device__ __forceinline__ comp_type div_i128(comp_type x, long long n) {
+  const bool neg = x < 0;
+  unsigned __int128 a = neg ? (unsigned __int128)(-x) : (unsigned __int128)x;
+  unsigned long long rem = 0;
+  unsigned __int128 q = 0;
+  for (int i = 3; i >= 0; --i) {
+    const unsigned long long cur = (rem << 32) | (unsigned long long)((a >> (32 * i)) & 0xffffffffull);
+    q |= (unsigned __int128)(cur / (unsigned long long)n) << (32 * i);
+    rem = cur % (unsigned long long)n;
+  }
+  return neg ? -(comp_type)q : (comp_type)q;
+}
+
+__device__ __forceinline__ comp_type block_sum_i128(comp_type v, comp_type* red) {
+  v = warp_sum_i128(v);
+  const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[w] = v;
+  __syncthreads();
+  comp_type t = 0;
+  for (int i = 0; i < nw; ++i) t += red[i];
+  return t;
+}
+
+// local index of padded node v in the sorted region list, or -1
+__device__ __forceinline__ int local_index(const int* sn, int n, int v) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (sn[mid] < v) lo = mid + 1; else hi = mid;
+  }
+  return (lo < n && sn[lo] == v) ? lo : -1;
+}
+
+// status[0]: 0 done, 1 the epoch cap ended the max-flow (the caller probes
+// again with the lattice-wide solver); acc as k_seg_probe
+__global__ void __launch_bounds__(1024)
+    k_region_probe(const int* nodes, int n, int key, const int* keys, Geo g, Stencil st, dtype lm,
+                   int pull, unsigned long long qii_lo, unsigned long long qii_hi,
+                   const dtype* base, dtype* cur, dtype* off, dtype* exc, dtype* res,
+                   unsigned char* lab, unsigned long long* acc, int* status, int max_epochs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int K = st.K;
+  dtype* e = reinterpret_cast<dtype*>(smem);                  // [n] excess
+  dtype* inflow = e + n;                                      // [n]
+  comp_type* red = reinterpret_cast<comp_type*>(inflow + n);  // [32]
+  int* sn = reinterpret_cast<int*>(red + 32);                 // [n] padded ids, ascending
+  int* h = sn + n;                                            // [n] heights
+  short* nbr = reinterpret_cast<short*>(h + n);               // [n * K] local neighbours or -1
+  __shared__ dtype s_off;
+  const int T = blockDim.x;
+
+  // 1. the region, its influence sum and the offset (setRegionToLambda)
+  comp_type gsum = 0;
+  for (int j = threadIdx.x; j < n; j += T) {
+    const int i = nodes[j];
+    sn[j] = i;
+    gsum += comp_type(-exc[i]) + off[i] - cur[i];
+  }
+  gsum = block_sum_i128(gsum, red);
+  if (threadIdx.x == 0) {
+    const comp_type qii = (comp_type)(((unsigned __int128)qii_hi << 64) | qii_lo);
+    comp_type t = comp_type(mult_fv_scale(qii, lm)) + gsum;
+    if (t < 0) t -= (n - 1);  // floorAverage
+    s_off = dtype(div_i128(t, n));
+  }
+  __syncthreads();
+  const dtype fv_offset = s_off;
+  for (int j = threadIdx.x; j < n; j += T) {
+    const int i = sn[j];
+    const dtype fv = mult_fv_scale(base[i], lm);
+    const dtype o = fv_offset + ((pull && fv > fv_offset) ? 1 : 0);
+    const dtype ex = exc[i] - ((fv - o) - (cur[i] - off[i]));
+    cur[i] = fv;
+    off[i] = o;
+    e[j] = ex;
+    inflow[j] = 0;
+    const int c = i % g.Cp, b = i / g.Cp;
+    for (int k = 0; k < K; ++k) {
+      const int nb = b + st.db[k], nc = c + st.dc[k];
+      int loc = -1;
+      if (nb >= 0 && nb < g.B && nc >= 0 && nc < g.C) {
+        const int v = nb * g.Cp + nc;
+        if (keys[v] == key) loc = local_index(sn, n, v);
+      }
+      nbr[j * K + k] = short(loc);
+    }
+  }
+  __syncthreads();
+
+  // 2. the region's max-flow
+  int epoch = 0;
+  for (;; ++epoch) {
+    // exact distance to the nearest deficit along residual edges
+    for (int j = threadIdx.x; j < n; j += T) h[j] = e[j] < 0 ? 0 : kHUnreached;
+    __syncthreads();
+    // (a node found on this level is set to lvl + 1, which no other test of
+    // the same level matches, so the level needs no barrier inside)
+    for (int lvl = 0; lvl < n; ++lvl) {
+      int changed = 0;
+      for (int j = threadIdx.x; j < n; j += T) {
+        if (h[j] != kHUnreached) continue;
+        const int i = sn[j];
+        for (int k = 0; k < K; ++k) {
+          const int v = nbr[j * K + k];
+          if (v >= 0 && h[v] == lvl && res[(long long)k * g.NP + i] > 0) {
+            h[j] = lvl + 1;
+            changed = 1;
+            break;
+          }
+        }
+      }
+      if (!__syncthreads_or(changed)) break;
+    }
+    int act = 0;
+    for (int j = threadIdx.x; j < n; j += T) act |= (e[j] > 0 && h[j] < kHUnreached);
+    if (!__syncthreads_or(act)) break;
+    if (epoch >= max_epochs) {
+      if (threadIdx.x == 0) status[0] = 1;
+      break;
+    }
+    // push / relabel sweeps on these labels
+    for (int sweep = 0; sweep < 8; ++sweep) {
+      for (int j = threadIdx.x; j < n; j += T) {
+        dtype rem = e[j];
+        const int hj = h[j];
+        if (rem <= 0 || hj >= kHUnreached || hj == 0) continue;
+        const int i = sn[j];
+        for (int k = 0; k < K && rem > 0; ++k) {
+          const int v = nbr[j * K + k];
+          if (v < 0 || h[v] != hj - 1) continue;
+          const dtype r = res[(long long)k * g.NP + i];
+          if (r <= 0) continue;
+          const dtype a = r < rem ? r : rem;
+          res[(long long)k * g.NP + i] = r - a;
+          res[(long long)st.rev[k] * g.NP + sn[v]] += a;
+          atomicAdd(reinterpret_cast<unsigned long long*>(&inflow[v]), (unsigned long long)a);
+          rem -= a;
+        }
+        e[j] = rem;
+      }
+      __syncthreads();
+      for (int j = threadIdx.x; j < n; j += T) {
+        e[j] += inflow[j];
+        inflow[j] = 0;
+      }
+      __syncthreads();
+      // relabel: a node still holding excess moves one above its lowest
+      // residual neighbour
+      for (int j = threadIdx.x; j < n; j += T) {
+        if (e[j] <= 0 || h[j] >= kHUnreached || h[j] == 0) continue;
+        const int i = sn[j];
+        int hm = kHUnreached;
+        for (int k = 0; k < K; ++k) {
+          const int v = nbr[j * K + k];
+          if (v >= 0 && res[(long long)k * g.NP + i] > 0) hm = min(hm, h[v]);
+        }
+        if (hm != h[j] - 1) h[j] = hm >= kHUnreached - 1 ? kHUnreached : hm + 1;
+      }
+      __syncthreads();
+    }
+  }
+
+  // 3. read-out: labels, per-side sums, cut value; excess back to the lattice
+  comp_type g0 = 0, g1 = 0, cv = 0;
+  int ons = 0;
+  for (int j = threadIdx.x; j < n; j += T) {
+    const int i = sn[j];
+    exc[i] = e[j];
+    const bool on = h[j] >= kHUnreached;
+    lab[j] = on ? 1 : 0;
+    const comp_type gam = comp_type(-e[j]) + off[i] - cur[i];
+    if (on) {
+      g1 += gam;
+      ++ons;
+    } else {
+      g0 += gam;
+      for (int k = 0; k < K; ++k) {
+        const int v = nbr[j * K + k];
+        if (v >= 0 && h[v] >= kHUnreached) {
+          const dtype a = res[(long long)k * g.NP + i];
+          cv += (a < 0 ? -a : a) >> 1;
+        }
+      }
+    }
+  }
+  g0 = block_sum_i128(g0, red);
+  g1 = block_sum_i128(g1, red);
+  cv = block_sum_i128(cv, red);
+  const comp_type on_total = block_sum_i128(comp_type(ons), red);
+  if (threadIdx.x == 0) {
+    acc[0] = (unsigned long long)g0;
+    acc[1] = (unsigned long long)(g0 >> 64);
+    acc[2] = (unsigned long long)g1;
+    acc[3] = (unsigned long long)(g1 >> 64);
+    acc[4] = (unsigned long long)cv;
+    acc[5] = (unsigned long long)(cv >> 64);
+    acc[6] = (unsigned long long)on_total;
+  }
+}
+
+constexpr size_t kRegionProbeSmem = 200 * 1024;
+
+size_t region_probe_smem(int n, int K) {
+  return size_t(n) * (8 + 8 + 4 + 4 + 2 * K) + 32 * sizeof(comp_type) + 16;
+}
+
 __global__ void k_seg_setkey(const int* nodes, int n, int key, int* keys) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < n) keys[nodes[j]] = key;
@@ -352,6 +575,12 @@ class PathGPU {
   comp_type region_gamma(const Seg& sg);
   void set_region_to_lambda(Seg& sg, dtype lambda, bool pull);
   CutPtr probe(Seg& sg);
+  // setRegionToLambda + runPartitionedSection: one fused launch for a small
+  // region, else the lattice-wide solver
+  CutPtr region_probe(Seg& sg, dtype lambda, bool pull);
+  CutPtr read_probe(Seg& sg);
+  int* d_status = nullptr;
+  int small_cap = 0;  // largest region the fused probe takes
   dtype lambda_of_join(int a, int b, dtype cur) const;
   dtype calculate_joins(int a, int b, dtype cur);
   dtype first_join_point(const Seg& sg) const {
@@ -389,6 +618,16 @@ PathGPU::PathGPU(Engine& e, const std::vector<int64_t>& base_rowmajor,
   ck(cudaMalloc(&d_keys, NP * sizeof(int)), "cudaMalloc");
   ck(cudaMalloc(&d_lab, std::max<long long>(E.N, 1)), "cudaMalloc");
   ck(cudaMalloc(&d_acc, 8 * sizeof(unsigned long long)), "cudaMalloc");
+  ck(cudaMalloc(&d_status, sizeof(int)), "cudaMalloc");
+  {
+    // the fused probe's region bound: what fits the shared memory of a block
+    small_cap = kSmallRegion;
+    while (small_cap > 32 && region_probe_smem(small_cap, K) > kRegionProbeSmem) small_cap /= 2;
+    // one value for every kernel size, so that concurrent paths agree
+    ck(cudaFuncSetAttribute(k_region_probe, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            int(kRegionProbeSmem)),
+       "cudaFuncSetAttribute");
+  }
   ck(cudaMallocHost(&h_acc, 8 * sizeof(unsigned long long)), "cudaMallocHost");
   ck(cudaMallocHost(&h_lab, std::max<long long>(E.N, 1)), "cudaMallocHost");
   ck(cudaMemcpyAsync(d_base, base.data(), NP * sizeof(dtype), cudaMemcpyHostToDevice, s), "memcpy");
@@ -411,6 +650,7 @@ PathGPU::~PathGPU() {
   cudaFree(d_keys);
   cudaFree(d_lab);
   cudaFree(d_acc);
+  cudaFree(d_status);
   cudaFreeHost(h_acc);
   cudaFreeHost(h_lab);
 }
@@ -504,6 +744,11 @@ CutPtr PathGPU::probe(Seg& sg) {
   ck(E.counted(cudaGetLastError()), "segment probe");
   k_seg_kmask<<<nblk(n, 256), 256, 0, s>>>(sg.d_nodes, n, sg.key, d_keys, g, st, E.d_kmask, 0);
   ck(E.counted(cudaGetLastError()), "segment mask");
+  return read_probe(sg);
+}
+
+CutPtr PathGPU::read_probe(Seg& sg) {
+  const int n = int(sg.ci_nodes.size());
   ck(cudaMemcpyAsync(h_lab, d_lab, (size_t)n, cudaMemcpyDeviceToHost, s), "memcpy");
   read_acc();
   CutPtr cut = std::make_shared<Cut>();
@@ -514,6 +759,31 @@ CutPtr PathGPU::probe(Seg& sg) {
   cut->part[1].reserve(size_t(on));
   for (int j = 0; j < n; ++j) cut->part[h_lab[j] ? 1 : 0].push_back(sg.ci_nodes[j]);
   cut->cut_value = dtype(read_i128(2));
+  return cut;
+}
+
+CutPtr PathGPU::region_probe(Seg& sg, dtype lambda, bool pull) {
+  const int n = int(sg.ci_nodes.size());
+  if (n > small_cap) {
+    set_region_to_lambda(sg, lambda, pull);
+    return probe(sg);
+  }
+  ++stats[1];
+  ck(cudaMemsetAsync(d_status, 0, sizeof(int), s), "memset");
+  const int threads = std::min(1024, std::max(32, (n + 31) / 32 * 32));
+  k_region_probe<<<1, threads, region_probe_smem(n, K), s>>>(
+      sg.d_nodes, n, sg.key, d_keys, g, st, lambda, pull ? 1 : 0,
+      (unsigned long long)sg.qii_sum, (unsigned long long)(sg.qii_sum >> 64), d_base, d_cur,
+      d_off, (dtype*)E.d_exc, (dtype*)E.d_res, d_lab, d_acc, d_status, 4 * n + 64);
+  ck(E.counted(cudaGetLastError()), "region probe");
+  int status = 0;
+  ck(cudaMemcpyAsync(&h_acc[7], d_status, sizeof(int), cudaMemcpyDeviceToHost, s), "memcpy");
+  CutPtr cut = read_probe(sg);
+  std::memcpy(&status, &h_acc[7], sizeof(int));
+  if (status) {  // the epoch cap ended it: finish on the lattice-wide solver
+    --stats[1];
+    return probe(sg);
+  }
   return cut;
 }
 
@@ -559,8 +829,7 @@ PathGPU::DSI PathGPU::bisection_check(Seg& sg, dtype lb, dtype ub) {
   bool occurred = false;
   while (lb + 1 < ub) {
     const dtype t = rate != 1 ? (lb + 1) + ((ub - (lb + 1)) / (dtype(1) << rate)) : (ub + lb) / 2;
-    set_region_to_lambda(sg, t, true);
-    CutPtr cut = probe(sg);
+    CutPtr cut = region_probe(sg, t, true);
     if (!cut->any_cut) {
       ub = t;
     } else {
@@ -579,8 +848,7 @@ PathGPU::DSI PathGPU::bisection_check(Seg& sg, dtype lb, dtype ub) {
 
 // TVRegPathSegment::_calculateSingleSplit (tv_regpath_node.hpp:457-633)
 PathGPU::DSI PathGPU::single_split(Seg& sg, const dtype lambda_lb, const dtype lambda_ub) {
-  set_region_to_lambda(sg, lambda_lb, false);
-  CutPtr cut = probe(sg);
+  CutPtr cut = region_probe(sg, lambda_lb, false);
   DSI d;
   if (!cut->any_cut) return d;
   const dtype s0 = dtype(cut->part[0].size()), s1 = dtype(cut->part[1].size());
