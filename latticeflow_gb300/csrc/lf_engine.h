@@ -144,8 +144,10 @@ int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lam
           int64_t* levels_out, int32_t* sets_out = nullptr);
 void tv_fill_single(Engine& E, const double* f, double lambda, double* mean, double* scale,
                     std::vector<int64_t>* base_fv, std::vector<long long>* pwf2_out);
-// the reference's regularisation path (lf_tvpath.cu); stats (may be null):
-// [0] path segments, [1] region probes, [2] events, [3] initial level sets
+// the reference's regularisation path (lf_tvpath.cu); stats (may be null,
+// else 8 entries): [0] path segments, [1] region probes, [2] events, [3]
+// initial level sets, [4] probes on the lattice-wide solver, [5]-[7]
+// microseconds in those probes, in fused probes, in segment set-ups
 int tv_2d_path(const KernelDef* kd, size_t nx, size_t ny, const double* f, size_t n_lambda,
                const double* lambdas, double* out, int64_t* stats);
 int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* levels_out);

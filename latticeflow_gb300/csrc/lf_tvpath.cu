@@ -276,7 +276,10 @@ __device__ __forceinline__ int local_index(const int* sn, int n, int v) {
 }
 
 // status[0]: 0 done, 1 the epoch cap ended the max-flow (the caller probes
-// again with the lattice-wide solver); acc as k_seg_probe
+// again with the lattice-wide solver); acc as k_seg_probe.  Shared memory:
+// excess, inflow and the residuals of every node in each direction (local
+// layout j * K + k), then the 128-bit reduction slots, the padded ids, the
+// heights and the local neighbour table.
 __global__ void __launch_bounds__(1024)
     k_region_probe(const int* nodes, int n, int key, const int* keys, Geo g, Stencil st, dtype lm,
                    int pull, unsigned long long qii_lo, unsigned long long qii_hi,
@@ -284,12 +287,14 @@ __global__ void __launch_bounds__(1024)
                    unsigned char* lab, unsigned long long* acc, int* status, int max_epochs) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int K = st.K;
-  dtype* e = reinterpret_cast<dtype*>(smem);                  // [n] excess
-  dtype* inflow = e + n;                                      // [n]
-  comp_type* red = reinterpret_cast<comp_type*>(inflow + n);  // [32]
-  int* sn = reinterpret_cast<int*>(red + 32);                 // [n] padded ids, ascending
-  int* h = sn + n;                                            // [n] heights
-  short* nbr = reinterpret_cast<short*>(h + n);               // [n * K] local neighbours or -1
+  const int n2 = (n + 1) & ~1;
+  dtype* e = reinterpret_cast<dtype*>(smem);                  // [n2] excess
+  dtype* inflow = e + n2;                                     // [n2]
+  dtype* rs = inflow + n2;                                    // [n2 * K] residuals
+  comp_type* red = reinterpret_cast<comp_type*>(rs + (size_t)n2 * K);  // [32]
+  int* sn = reinterpret_cast<int*>(red + 32);                 // [n2] padded ids, ascending
+  int* h = sn + n2;                                           // [n2] heights
+  short* nbr = reinterpret_cast<short*>(h + n2);              // [n2 * K] local neighbours or -1
   __shared__ dtype s_off;
   const int T = blockDim.x;
 
@@ -327,26 +332,26 @@ __global__ void __launch_bounds__(1024)
         if (keys[v] == key) loc = local_index(sn, n, v);
       }
       nbr[j * K + k] = short(loc);
+      rs[j * K + k] = res[(long long)k * g.NP + i];
     }
   }
   __syncthreads();
 
-  // 2. the region's max-flow
+  // 2. the region's max-flow on the staged residuals
   int epoch = 0;
   for (;; ++epoch) {
-    // exact distance to the nearest deficit along residual edges
+    // exact distance to the nearest deficit along residual edges (a node
+    // found on a level is set to lvl + 1, which no other test of the same
+    // level matches, so a level needs no barrier inside)
     for (int j = threadIdx.x; j < n; j += T) h[j] = e[j] < 0 ? 0 : kHUnreached;
     __syncthreads();
-    // (a node found on this level is set to lvl + 1, which no other test of
-    // the same level matches, so the level needs no barrier inside)
     for (int lvl = 0; lvl < n; ++lvl) {
       int changed = 0;
       for (int j = threadIdx.x; j < n; j += T) {
         if (h[j] != kHUnreached) continue;
-        const int i = sn[j];
         for (int k = 0; k < K; ++k) {
           const int v = nbr[j * K + k];
-          if (v >= 0 && h[v] == lvl && res[(long long)k * g.NP + i] > 0) {
+          if (v >= 0 && h[v] == lvl && rs[j * K + k] > 0) {
             h[j] = lvl + 1;
             changed = 1;
             break;
@@ -362,21 +367,22 @@ __global__ void __launch_bounds__(1024)
       if (threadIdx.x == 0) status[0] = 1;
       break;
     }
-    // push / relabel sweeps on these labels
+    // push / relabel sweeps on these labels: a push from j to a neighbour
+    // one level down; that neighbour pushes only further down, so the
+    // reverse residual is written by j alone
     for (int sweep = 0; sweep < 8; ++sweep) {
       for (int j = threadIdx.x; j < n; j += T) {
         dtype rem = e[j];
         const int hj = h[j];
         if (rem <= 0 || hj >= kHUnreached || hj == 0) continue;
-        const int i = sn[j];
         for (int k = 0; k < K && rem > 0; ++k) {
           const int v = nbr[j * K + k];
           if (v < 0 || h[v] != hj - 1) continue;
-          const dtype r = res[(long long)k * g.NP + i];
+          const dtype r = rs[j * K + k];
           if (r <= 0) continue;
           const dtype a = r < rem ? r : rem;
-          res[(long long)k * g.NP + i] = r - a;
-          res[(long long)st.rev[k] * g.NP + sn[v]] += a;
+          rs[j * K + k] = r - a;
+          rs[v * K + st.rev[k]] += a;
           atomicAdd(reinterpret_cast<unsigned long long*>(&inflow[v]), (unsigned long long)a);
           rem -= a;
         }
@@ -388,15 +394,14 @@ __global__ void __launch_bounds__(1024)
         inflow[j] = 0;
       }
       __syncthreads();
-      // relabel: a node still holding excess moves one above its lowest
-      // residual neighbour
+      // relabel: a node still holding excess and no admissible edge moves
+      // one above its lowest residual neighbour
       for (int j = threadIdx.x; j < n; j += T) {
         if (e[j] <= 0 || h[j] >= kHUnreached || h[j] == 0) continue;
-        const int i = sn[j];
         int hm = kHUnreached;
         for (int k = 0; k < K; ++k) {
           const int v = nbr[j * K + k];
-          if (v >= 0 && res[(long long)k * g.NP + i] > 0) hm = min(hm, h[v]);
+          if (v >= 0 && rs[j * K + k] > 0) hm = min(hm, h[v]);
         }
         if (hm != h[j] - 1) h[j] = hm >= kHUnreached - 1 ? kHUnreached : hm + 1;
       }
@@ -404,12 +409,13 @@ __global__ void __launch_bounds__(1024)
     }
   }
 
-  // 3. read-out: labels, per-side sums, cut value; excess back to the lattice
+  // 3. read-out: labels, per-side sums, cut value; excess and residuals back
   comp_type g0 = 0, g1 = 0, cv = 0;
   int ons = 0;
   for (int j = threadIdx.x; j < n; j += T) {
     const int i = sn[j];
     exc[i] = e[j];
+    for (int k = 0; k < K; ++k) res[(long long)k * g.NP + i] = rs[j * K + k];
     const bool on = h[j] >= kHUnreached;
     lab[j] = on ? 1 : 0;
     const comp_type gam = comp_type(-e[j]) + off[i] - cur[i];
@@ -421,7 +427,7 @@ __global__ void __launch_bounds__(1024)
       for (int k = 0; k < K; ++k) {
         const int v = nbr[j * K + k];
         if (v >= 0 && h[v] >= kHUnreached) {
-          const dtype a = res[(long long)k * g.NP + i];
+          const dtype a = rs[j * K + k];
           cv += (a < 0 ? -a : a) >> 1;
         }
       }
@@ -445,7 +451,8 @@ __global__ void __launch_bounds__(1024)
 constexpr size_t kRegionProbeSmem = 200 * 1024;
 
 size_t region_probe_smem(int n, int K) {
-  return size_t(n) * (8 + 8 + 4 + 4 + 2 * K) + 32 * sizeof(comp_type) + 16;
+  const size_t n2 = size_t((n + 1) & ~1);
+  return n2 * (8 + 8 + 8 * size_t(K) + 4 + 4 + 2 * size_t(K)) + 32 * sizeof(comp_type) + 16;
 }
 
 __global__ void k_seg_setkey(const int* nodes, int n, int key, int* keys) {
@@ -497,7 +504,10 @@ class PathGPU {
   ~PathGPU();
   void run();
   int output(const std::vector<double>& lams, double* out);
-  int64_t stats[4] = {0, 0, 0, 0};
+  // [0] segments, [1] probes, [2] events, [3] initial level sets, [4] probes
+  // on the lattice-wide solver, [5] microseconds in them, [6] microseconds in
+  // fused probes, [7] microseconds in segment set-ups
+  int64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
  private:
   enum Mode { Unset, Initial, Join, Split };
@@ -637,6 +647,10 @@ PathGPU::PathGPU(Engine& e, const std::vector<int64_t>& base_rowmajor,
   ck(cudaMemsetAsync(d_keys, 0xff, NP * sizeof(int), s), "memset");
   // no node solves until a probe marks its region
   ck(cudaMemsetAsync(E.d_kmask, 0, NP * sizeof(uint64_t), s), "memset");
+  // a region probe moves flow within one region, a small part of the
+  // lattice: a short pass cadence between relabels (the parametric flow's
+  // 64 passes are for sections that span the lattice)
+  E.tune.launches_per_relabel = 8;
   ck(cudaStreamSynchronize(s), "sync");
 }
 
@@ -688,6 +702,7 @@ void PathGPU::read_acc() {
 // of two int64 sums (getRegionInfo, tv_regpath_node.hpp:176-206), i.e. the
 // exact sum taken modulo 2^64.
 void PathGPU::sync_information(Seg& sg, dtype lambda) {
+  const auto t0 = std::chrono::steady_clock::now();
   const int n = int(sg.ci_nodes.size());
   sg.n_nodes = size_t(n);
   ck(cudaMemsetAsync(d_acc, 0, 7 * sizeof(unsigned long long), s), "memset");
@@ -699,6 +714,8 @@ void PathGPU::sync_information(Seg& sg, dtype lambda) {
   const comp_type adj = comp_type(1) << kAdjustBits;
   sg.ar0 = dtype((gamma * adj) / comp_type(n));
   sg.ar1 = dtype(((sg.qii_sum + gamma) * adj) / comp_type(n));
+  stats[7] += (int64_t)std::chrono::duration_cast<std::chrono::microseconds>(
+                  std::chrono::steady_clock::now() - t0).count();
 }
 
 // TVRegPathSegment::get_r_AtLambda (tv_regpath_node.hpp:131-148)
@@ -764,9 +781,17 @@ CutPtr PathGPU::read_probe(Seg& sg) {
 
 CutPtr PathGPU::region_probe(Seg& sg, dtype lambda, bool pull) {
   const int n = int(sg.ci_nodes.size());
+  const auto t0 = std::chrono::steady_clock::now();
+  auto us = [&]() {
+    return (int64_t)std::chrono::duration_cast<std::chrono::microseconds>(
+               std::chrono::steady_clock::now() - t0).count();
+  };
   if (n > small_cap) {
     set_region_to_lambda(sg, lambda, pull);
-    return probe(sg);
+    CutPtr c = probe(sg);
+    ++stats[4];
+    stats[5] += us();
+    return c;
   }
   ++stats[1];
   ck(cudaMemsetAsync(d_status, 0, sizeof(int), s), "memset");
@@ -782,8 +807,12 @@ CutPtr PathGPU::region_probe(Seg& sg, dtype lambda, bool pull) {
   std::memcpy(&status, &h_acc[7], sizeof(int));
   if (status) {  // the epoch cap ended it: finish on the lattice-wide solver
     --stats[1];
-    return probe(sg);
+    ++stats[4];
+    cut = probe(sg);
+    stats[5] += us();
+    return cut;
   }
+  stats[6] += us();
   return cut;
 }
 
@@ -1234,7 +1263,7 @@ int tv_2d_path(const KernelDef* kd, size_t nx, size_t ny, const double* f, size_
   P.run();
   const int rc = P.output(lams, out);
   if (stats)
-    for (int i = 0; i < 4; ++i) stats[i] = P.stats[i];
+    for (int i = 0; i < 8; ++i) stats[i] = P.stats[i];
   return rc;
 }
 
