@@ -278,10 +278,11 @@ int lf_tv_2d_level_sets(const char* kernel, size_t nx, size_t ny, const double* 
  * lambda counts as 0 and n_lambda = 0 returns at once. */
 int lf_tv_2d_path(const char* kernel, size_t nx, size_t ny, const double* f, size_t n_lambda,
                   const double* lambdas, double* out);
-/* The same, with statistics (stats: 8 int64, may be NULL): path segments,
+/* The same, with statistics (stats: 10 int64, may be NULL): path segments,
  * region probes (device max-flows), events applied, initial level sets,
  * probes of regions too large for one block, and the microseconds spent in
- * those probes, in the one-block probes and in segment set-ups. */
+ * those probes, in the one-block probes and in segment set-ups, and the
+ * epochs and BFS levels run by the one-block probes. */
 int lf_tv_2d_path_stats(const char* kernel, size_t nx, size_t ny, const double* f,
                         size_t n_lambda, const double* lambdas, double* out, int64_t* stats);
 

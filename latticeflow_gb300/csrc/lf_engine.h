@@ -145,9 +145,10 @@ int tv_2d(const KernelDef* kd, size_t nx, size_t ny, const double* f, double lam
 void tv_fill_single(Engine& E, const double* f, double lambda, double* mean, double* scale,
                     std::vector<int64_t>* base_fv, std::vector<long long>* pwf2_out);
 // the reference's regularisation path (lf_tvpath.cu); stats (may be null,
-// else 8 entries): [0] path segments, [1] region probes, [2] events, [3]
+// else 10 entries): [0] path segments, [1] region probes, [2] events, [3]
 // initial level sets, [4] probes on the lattice-wide solver, [5]-[7]
-// microseconds in those probes, in fused probes, in segment set-ups
+// microseconds in those probes, in fused probes, in segment set-ups,
+// [8] [9] epochs and BFS levels of the fused probes
 int tv_2d_path(const KernelDef* kd, size_t nx, size_t ny, const double* f, size_t n_lambda,
                const double* lambdas, double* out, int64_t* stats);
 int tv_2d_on(Engine& E, const double* f, double lambda, double* out, int64_t* levels_out);

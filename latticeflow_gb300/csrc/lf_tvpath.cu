@@ -276,7 +276,8 @@ __device__ __forceinline__ int local_index(const int* sn, int n, int v) {
 }
 
 // status[0]: 0 done, 1 the epoch cap ended the max-flow (the caller probes
-// again with the lattice-wide solver); acc as k_seg_probe.  Shared memory:
+// again with the lattice-wide solver); status[1] / [2] count the epochs and
+// BFS levels run (summed over launches); acc as k_seg_probe.  Shared memory:
 // excess, inflow and the residuals of every node in each direction (local
 // layout j * K + k), then the 128-bit reduction slots, the padded ids, the
 // heights and the local neighbour table.
@@ -298,12 +299,24 @@ __global__ void __launch_bounds__(1024)
   __shared__ dtype s_off;
   const int T = blockDim.x;
 
-  // 1. the region, its influence sum and the offset (setRegionToLambda)
+  // 1. the region, its influence sum and the offset (setRegionToLambda).
+  // Every node id is checked against the lattice: a bad one sets
+  // status[3] and the block stops before touching anything.
   comp_type gsum = 0;
+  int bad = 0;
   for (int j = threadIdx.x; j < n; j += T) {
     const int i = nodes[j];
+    if (i < 0 || (long long)i >= g.NP || (j > 0 && nodes[j - 1] >= i)) {
+      bad = 1;
+      sn[j] = 0;
+      continue;
+    }
     sn[j] = i;
     gsum += comp_type(-exc[i]) + off[i] - cur[i];
+  }
+  if (__syncthreads_or(bad)) {
+    if (threadIdx.x == 0) status[3] = 1;
+    return;
   }
   gsum = block_sum_i128(gsum, red);
   if (threadIdx.x == 0) {
@@ -331,14 +344,14 @@ __global__ void __launch_bounds__(1024)
         const int v = nb * g.Cp + nc;
         if (keys[v] == key) loc = local_index(sn, n, v);
       }
-      nbr[j * K + k] = short(loc);
+      nbr[j * K + k] = short(loc >= 0 && loc < n ? loc : -1);
       rs[j * K + k] = res[(long long)k * g.NP + i];
     }
   }
   __syncthreads();
 
   // 2. the region's max-flow on the staged residuals
-  int epoch = 0;
+  int epoch = 0, levels = 0;
   for (;; ++epoch) {
     // exact distance to the nearest deficit along residual edges (a node
     // found on a level is set to lvl + 1, which no other test of the same
@@ -358,6 +371,7 @@ __global__ void __launch_bounds__(1024)
           }
         }
       }
+      ++levels;
       if (!__syncthreads_or(changed)) break;
     }
     int act = 0;
@@ -438,6 +452,8 @@ __global__ void __launch_bounds__(1024)
   cv = block_sum_i128(cv, red);
   const comp_type on_total = block_sum_i128(comp_type(ons), red);
   if (threadIdx.x == 0) {
+    status[1] += epoch;
+    status[2] += levels;
     acc[0] = (unsigned long long)g0;
     acc[1] = (unsigned long long)(g0 >> 64);
     acc[2] = (unsigned long long)g1;
@@ -627,8 +643,9 @@ PathGPU::PathGPU(Engine& e, const std::vector<int64_t>& base_rowmajor,
   ck(cudaMalloc(&d_off, NP * sizeof(dtype)), "cudaMalloc");
   ck(cudaMalloc(&d_keys, NP * sizeof(int)), "cudaMalloc");
   ck(cudaMalloc(&d_lab, std::max<long long>(E.N, 1)), "cudaMalloc");
-  ck(cudaMalloc(&d_acc, 8 * sizeof(unsigned long long)), "cudaMalloc");
-  ck(cudaMalloc(&d_status, sizeof(int)), "cudaMalloc");
+  ck(cudaMalloc(&d_acc, 8 * sizeof(unsigned long long)), "cudaMalloc");  // [7] unused
+  ck(cudaMalloc(&d_status, 4 * sizeof(int)), "cudaMalloc");
+  ck(cudaMemsetAsync(d_status, 0, 4 * sizeof(int), s), "memset");
   {
     // the fused probe's region bound: what fits the shared memory of a block
     small_cap = kSmallRegion;
@@ -638,7 +655,8 @@ PathGPU::PathGPU(Engine& e, const std::vector<int64_t>& base_rowmajor,
                             int(kRegionProbeSmem)),
        "cudaFuncSetAttribute");
   }
-  ck(cudaMallocHost(&h_acc, 8 * sizeof(unsigned long long)), "cudaMallocHost");
+  // [0..6] probe sums, [8..9] the probe's status words
+  ck(cudaMallocHost(&h_acc, 10 * sizeof(unsigned long long)), "cudaMallocHost");
   ck(cudaMallocHost(&h_lab, std::max<long long>(E.N, 1)), "cudaMallocHost");
   ck(cudaMemcpyAsync(d_base, base.data(), NP * sizeof(dtype), cudaMemcpyHostToDevice, s), "memcpy");
   // after the parametric flow: scale 1 (current value = base), offsets 0
@@ -651,6 +669,13 @@ PathGPU::PathGPU(Engine& e, const std::vector<int64_t>& base_rowmajor,
   // lattice: a short pass cadence between relabels (the parametric flow's
   // 64 passes are for sections that span the lattice)
   E.tune.launches_per_relabel = 8;
+  // region probes too large for one block run on the generic tile passes,
+  // without the tail step: a region probe is a max-flow confined to a
+  // small part of the lattice by its section mask, which those passes
+  // handle with no staging geometry
+  E.tune.pr_kernel = 1;
+  E.tune.bfs_kernel = 1;
+  E.tune.tail_active = -1;
   ck(cudaStreamSynchronize(s), "sync");
 }
 
@@ -679,6 +704,11 @@ int PathGPU::new_seg() {
 void PathGPU::upload_nodes(Seg& sg) {
   free_nodes(sg);
   const size_t n = sg.ci_nodes.size();
+  // every kernel over a region indexes the lattice with these ids
+  for (size_t j = 0; j < n; ++j)
+    if (sg.ci_nodes[j] < 0 || sg.ci_nodes[j] >= g.NP || (j > 0 && sg.ci_nodes[j - 1] >= sg.ci_nodes[j]))
+      throw LfError{6, "TV path: a region's node list is not a sorted list of lattice nodes"};
+  if (n == 0) throw LfError{6, "TV path: empty region"};
   ck(cudaMallocAsync(&sg.d_nodes, std::max<size_t>(n, 1) * sizeof(int), s), "cudaMallocAsync");
   ck(cudaMemcpyAsync(sg.d_nodes, sg.ci_nodes.data(), n * sizeof(int), cudaMemcpyHostToDevice, s),
      "memcpy");
@@ -794,18 +824,19 @@ CutPtr PathGPU::region_probe(Seg& sg, dtype lambda, bool pull) {
     return c;
   }
   ++stats[1];
-  ck(cudaMemsetAsync(d_status, 0, sizeof(int), s), "memset");
+  ck(cudaMemsetAsync(d_status, 0, sizeof(int), s), "memset");  // the cap flag; [1], [2] count on
   const int threads = std::min(1024, std::max(32, (n + 31) / 32 * 32));
   k_region_probe<<<1, threads, region_probe_smem(n, K), s>>>(
       sg.d_nodes, n, sg.key, d_keys, g, st, lambda, pull ? 1 : 0,
       (unsigned long long)sg.qii_sum, (unsigned long long)(sg.qii_sum >> 64), d_base, d_cur,
       d_off, (dtype*)E.d_exc, (dtype*)E.d_res, d_lab, d_acc, d_status, 4 * n + 64);
   ck(E.counted(cudaGetLastError()), "region probe");
-  int status = 0;
-  ck(cudaMemcpyAsync(&h_acc[7], d_status, sizeof(int), cudaMemcpyDeviceToHost, s), "memcpy");
+  int status[4] = {0, 0, 0, 0};
+  ck(cudaMemcpyAsync(&h_acc[8], d_status, 4 * sizeof(int), cudaMemcpyDeviceToHost, s), "memcpy");
   CutPtr cut = read_probe(sg);
-  std::memcpy(&status, &h_acc[7], sizeof(int));
-  if (status) {  // the epoch cap ended it: finish on the lattice-wide solver
+  std::memcpy(status, &h_acc[8], sizeof(status));
+  if (status[3]) throw LfError{6, "TV path: a region probe met an invalid node id"};
+  if (status[0]) {  // the epoch cap ended it: finish on the lattice-wide solver
     --stats[1];
     ++stats[4];
     cut = probe(sg);
@@ -1169,6 +1200,13 @@ void PathGPU::run() {
         break;
     }
   }
+  {
+    int cnt[4] = {0, 0, 0, 0};
+    ck(cudaMemcpyAsync(cnt, d_status, sizeof(cnt), cudaMemcpyDeviceToHost, s), "memcpy");
+    ck(cudaStreamSynchronize(s), "sync");
+    stats[8] = cnt[1];
+    stats[9] = cnt[2];
+  }
   Seg& last = segs.back();
   last.lhs_lambda = 0;
   last.lhs_mode = Initial;
@@ -1263,7 +1301,7 @@ int tv_2d_path(const KernelDef* kd, size_t nx, size_t ny, const double* f, size_
   P.run();
   const int rc = P.output(lams, out);
   if (stats)
-    for (int i = 0; i < 8; ++i) stats[i] = P.stats[i];
+    for (int i = 0; i < 10; ++i) stats[i] = P.stats[i];
   return rc;
 }
 

@@ -331,14 +331,15 @@ def calculate2dTVPath(f, lambdas, kernel="Full2d_4", return_stats=False):
         raise ValueError("lambdas must be a 1-d sequence")
     nx, ny = f.shape
     out = np.empty((lam.size, nx, ny), dtype=np.float64)
-    st = np.zeros(8, dtype=np.int64)
+    st = np.zeros(10, dtype=np.int64)
     N.check(N.lib().lf_tv_2d_path_stats(kernel.encode(), nx, ny, _p(f), lam.size, _p(lam),
                                         _p(out), _p(st)))
     if return_stats:
         return out, {"segments": int(st[0]), "probes": int(st[1]), "events": int(st[2]),
                      "level_sets": int(st[3]), "large_probes": int(st[4]),
                      "large_probe_s": st[5] * 1e-6, "small_probe_s": st[6] * 1e-6,
-                     "setup_s": st[7] * 1e-6}
+                     "setup_s": st[7] * 1e-6, "small_epochs": int(st[8]),
+                     "small_bfs_levels": int(st[9])}
     return out
 
 
