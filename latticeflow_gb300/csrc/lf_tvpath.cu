@@ -381,14 +381,16 @@ __global__ void __launch_bounds__(1024)
       if (threadIdx.x == 0) status[0] = 1;
       break;
     }
-    // push / relabel sweeps on these labels: a push from j to a neighbour
-    // one level down; that neighbour pushes only further down, so the
-    // reverse residual is written by j alone
-    for (int sweep = 0; sweep < 8; ++sweep) {
+    // push / relabel sweeps on these labels until no node below height n
+    // holds excess (a label of n or more cannot lead to a deficit), at most
+    // 64 per exact relabel.  A push goes from j to a neighbour one level
+    // down; that neighbour pushes only further down, so the reverse
+    // residual is written by j alone.
+    for (int sweep = 0; sweep < 64; ++sweep) {
       for (int j = threadIdx.x; j < n; j += T) {
         dtype rem = e[j];
         const int hj = h[j];
-        if (rem <= 0 || hj >= kHUnreached || hj == 0) continue;
+        if (rem <= 0 || hj >= n) continue;
         for (int k = 0; k < K && rem > 0; ++k) {
           const int v = nbr[j * K + k];
           if (v < 0 || h[v] != hj - 1) continue;
@@ -403,23 +405,26 @@ __global__ void __launch_bounds__(1024)
         e[j] = rem;
       }
       __syncthreads();
+      // take the inflow, then relabel: a node still holding excess with no
+      // admissible edge moves one above its lowest residual neighbour
+      // (neighbours' labels may be read while they rise: a stale, lower
+      // label keeps the labelling valid)
+      int busy = 0;
       for (int j = threadIdx.x; j < n; j += T) {
-        e[j] += inflow[j];
+        const dtype ej = e[j] + inflow[j];
+        e[j] = ej;
         inflow[j] = 0;
-      }
-      __syncthreads();
-      // relabel: a node still holding excess and no admissible edge moves
-      // one above its lowest residual neighbour
-      for (int j = threadIdx.x; j < n; j += T) {
-        if (e[j] <= 0 || h[j] >= kHUnreached || h[j] == 0) continue;
+        const int hj = h[j];
+        if (ej <= 0 || hj >= n) continue;  // (a filled deficit at 0 rises too)
         int hm = kHUnreached;
         for (int k = 0; k < K; ++k) {
           const int v = nbr[j * K + k];
           if (v >= 0 && rs[j * K + k] > 0) hm = min(hm, h[v]);
         }
-        if (hm != h[j] - 1) h[j] = hm >= kHUnreached - 1 ? kHUnreached : hm + 1;
+        if (hm != hj - 1) h[j] = hm >= n ? n : hm + 1;
+        busy |= h[j] < n;
       }
-      __syncthreads();
+      if (!__syncthreads_or(busy)) break;
     }
   }
 
