@@ -10,9 +10,9 @@ seeded input at full size:
 * 256^3 Full3d_26 volume cut: the same;
 * the 512-lattice batch of uneven 4- and 8-connected cuts, lattice by
   lattice: the same;
-* one single-lambda TV solve of the 1024 x 1024 polygon image: levels
-  the level-set partition and every level set's total exact, levels within
-  one raw unit (2^-41 of the function range), doubles within 1e-9 relative.
+* one single-lambda TV solve of the 1024 x 1024 polygon image: the
+  level-set partition and every level set's total exact, levels within one
+  raw unit (2^-41 of the function range), doubles within 1e-9 relative.
 """
 import numpy as np
 import pytest
