@@ -527,8 +527,10 @@ class PathGPU {
   int output(const std::vector<double>& lams, double* out);
   // [0] segments, [1] probes, [2] events, [3] initial level sets, [4] probes
   // on the lattice-wide solver, [5] microseconds in them, [6] microseconds in
-  // fused probes, [7] microseconds in segment set-ups
-  int64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // fused probes, [7] microseconds in segment set-ups, [8] [9] epochs and BFS
+  // levels of the fused probes
+  static constexpr int kStats = 10;
+  int64_t stats[kStats] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 
  private:
   enum Mode { Unset, Initial, Join, Split };
@@ -1306,7 +1308,7 @@ int tv_2d_path(const KernelDef* kd, size_t nx, size_t ny, const double* f, size_
   P.run();
   const int rc = P.output(lams, out);
   if (stats)
-    for (int i = 0; i < 10; ++i) stats[i] = P.stats[i];
+    for (int i = 0; i < PathGPU::kStats; ++i) stats[i] = P.stats[i];
   return rc;
 }
 
