@@ -12,6 +12,13 @@ push-relabel to a maximum preflow, both canonical cut sets, flow value.
          inside the step); --e2e-handles N solves on N handles at once, one
          host thread each, so that transfers overlap other solves
 
+The default line also carries: parity (the timed workload's energy and
+both cut sets against the oracle), batched_vs_plain (the 512-lattice batch
+against 512 plain solves), tv_single_1024 (single-lambda TV of the 1024^2
+polygon image through the public call, beside the restated reference on one
+core) and serve (p50 / p99 latency of a short Poisson stream of TV
+requests).  --workload tv_path times the regularisation path.
+
 Multi-GPU: independent replicas (the path has no exchange step); value is the
 solves of all ranks over the max-over-ranks time ("scaling": "weak").
 
@@ -51,6 +58,10 @@ def parse():
     ap.add_argument("--max-group", type=int, default=8,
                     help="serve: largest group of same-shape TV requests solved together")
     ap.add_argument("--batch-size", type=int, default=512)
+    ap.add_argument("--tv-n", type=int, default=256,
+                    help="tv_path: side of the TV image (config 5 names 1024)")
+    ap.add_argument("--no-tv-summary", action="store_true",
+                    help="skip the single-lambda TV and serving summaries of the default run")
     ap.add_argument("--no-batch-summary", action="store_true",
                     help="skip the batched-vs-plain summary of the default run")
     ap.add_argument("--no-autotune", action="store_true")
@@ -433,6 +444,9 @@ def run_ours(args):
         if not args.no_batch_summary and not args.profile_run:
             del L
             out["batched_vs_plain"] = batch_summary(args)
+        if not args.no_tv_summary and not args.profile_run:
+            out["tv_single_1024"] = tv_single_summary()
+            out["serve"] = serve_summary(args)
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist
@@ -642,7 +656,6 @@ def run_serve(args):
         print(json.dumps(out))
 
 
-TV_PATH_N = 1024
 TV_PATH_LAMBDAS = 64
 
 
@@ -651,30 +664,33 @@ def tv_path_lambdas():
     return np.array([1e-3 * 1000.0 ** (i / (TV_PATH_LAMBDAS - 1)) for i in range(TV_PATH_LAMBDAS)])
 
 
-def tv_path_cpu_baseline(f, lams, budget_s=20.0):
-    """Restated reference single-lambda TV on one host core: lambdas taken
-    spread over the path until the budget is spent."""
+def tv_path_cpu_baseline(n, lams, seed, budget_s=30.0):
+    """The restated reference path tracker on one host core, on the largest
+    image of side n, n/2, n/4, ... whose path its time on a 64x64 image,
+    scaled by the fourth power of the side (its observed growth), puts
+    within the budget."""
     from oracle import oracle as O
+    from latticeflow_gb300 import workloads as W
     O.build_port()
-    order = [len(lams) // 2, len(lams) - 1, 0, len(lams) // 4, 3 * len(lams) // 4]
-    secs = []
-    t0 = time.time()
-    for i in order:
-        if secs and time.time() - t0 > budget_s:
-            break
-        _, _, s = O.port_tv_single("Full2d_4", f, float(lams[i]))
-        secs.append(s)
-    return {"value": round(len(secs) / sum(secs), 5), "unit": "lambda solves/s", "cores": 1,
-            "kind": "port",
-            "sample": "%d single-lambda solves of the %dx%d image at lambdas spread over the path "
-                      "(reference parametric flow restated, oracle/lf_oracle.cpp), %.1f s total"
-                      % (len(secs), f.shape[0], f.shape[1], sum(secs))}
+    _, t64, _ = O.port_tv_path("Full2d_4", W.tv_image(seed, n=64, polygons=30), lams)
+    m = n
+    while m > 64 and t64 * (m / 64.0) ** 4 > budget_s:
+        m //= 2
+    f = W.tv_image(seed, n=m, polygons=30)
+    _, secs, segs = O.port_tv_path("Full2d_4", f, lams)
+    return {"value": round(1.0 / secs, 5), "unit": "paths/s", "cores": 1, "kind": "port",
+            "sample": "one %d-lambda path of the %dx%d image (%d segments), the reference's "
+                      "path tracker restated (oracle/lf_oracle.cpp), %.2f s%s"
+                      % (len(lams), m, m, segs, secs,
+                         "" if m == n else "; the %dx%d path is beyond the budget" % (n, n)),
+            "side": m}
 
 
 def run_tv_path(args):
-    """--workload tv_path: the 1024x1024 Full2d_4 TV image at 64 lambdas
-    (calculate2dTVPath, host arrays in and out).  A step is one whole path;
-    value = lambda solves per second."""
+    """--workload tv_path: the regularisation path (calculate2dTVPath, the
+    reference's path tracker with its region probes on the GPU) of an
+    --tv-n square polygon image at 64 lambdas, host arrays in and out.  A
+    step is one whole path; value = paths per second."""
     import torch
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
@@ -685,7 +701,8 @@ def run_tv_path(args):
     _build.build_native()
     import latticeflow_gb300 as lf
     from latticeflow_gb300 import workloads as W
-    f = W.tv_image(args.seed, n=TV_PATH_N, polygons=30)
+    n = args.tv_n
+    f = W.tv_image(args.seed, n=n, polygons=30)
     lams = tv_path_lambdas()
     for _ in range(args.warmup):
         lf.calculate2dTVPath(f, lams)
@@ -696,30 +713,94 @@ def run_tv_path(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        P = lf.calculate2dTVPath(f, lams)
+        P, st = lf.calculate2dTVPath(f, lams, return_stats=True)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
     wall = max_over_ranks(wall)
-    value = replica_value(args.steps * len(lams), world, wall)
+    value = replica_value(args.steps, world, wall)
     out = {
-        "metric": METRIC, "value": round(value, 3), "unit": "lambda solves/s",
+        "metric": METRIC, "value": round(value, 5), "unit": "paths/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * wall / args.steps, 2), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int64",
         "data": "synthetic (seeded polygon image, latticeflow_gb300/workloads.py)",
-        "config": {"workload": "tv_path", "kernel": "Full2d_4", "shape": [TV_PATH_N, TV_PATH_N],
+        "config": {"workload": "tv_path", "kernel": "Full2d_4", "shape": [n, n],
                    "lambdas": "64 values 1e-3*1000^(i/63)", "seed": args.seed,
-                   "l2": "inputs larger than L2 (no flush needed)",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "e2e": {"value": round(value, 3), "unit": "lambda solves/s",
+        "e2e": {"value": round(value, 5), "unit": "paths/s",
                 "h2d_bytes_per_step": int(f.nbytes), "d2h_bytes_per_step": int(P.nbytes),
                 "note": "the step is the public host-array call itself"},
+        "path": {k: (round(float(v), 3) if isinstance(v, float) else v) for k, v in st.items()},
         "clocks": clocks,
     }
     if rank == 0:
-        out["cpu_baseline"] = tv_path_cpu_baseline(f, lams)
+        out["cpu_baseline"] = tv_path_cpu_baseline(n, lams, args.seed)
         print(json.dumps(out))
+
+
+def tv_single_summary(lams=(1e-3, 0.05, 1.0), n=1024):
+    """Single-lambda TV of the 1024x1024 polygon image through the public
+    call (host arrays), at three lambdas; the restated reference solve of
+    the middle one on one host core, and its parity."""
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    from oracle import oracle as O
+    f = W.tv_image(0, n=n, polygons=30)
+    lf.calculate2dTV(f[:64, :64], 0.05)  # loads the kernels
+    secs, outs = [], []
+    for lam in lams:
+        t0 = time.perf_counter()
+        outs.append(lf.calculate2dTV(f, lam))
+        secs.append(time.perf_counter() - t0)
+    O.build_port()
+    mid = len(lams) // 2
+    ref, _, cpu_s = O.port_tv_single("Full2d_4", f, lams[mid])
+    ok = float(np.abs(outs[mid] - ref).max()) <= 1e-9 * max(1.0, float(np.abs(ref).max()))
+    return {"shape": [n, n], "lambdas": list(lams), "s_per_lambda": [round(x, 4) for x in secs],
+            "mean_s": round(float(np.mean(secs)), 4),
+            "cpu_port_s": round(cpu_s, 3), "cpu_port_lambda": lams[mid], "cpu_cores": 1,
+            "parity": bool(ok),
+            "timing": "host clock around the public call (host arrays in and out)"}
+
+
+def serve_summary(args, requests=30, rate=1.0, workers=4):
+    """A short Poisson stream of single-lambda TV requests (config 5 sizes
+    {128..2048}^2, lambda log-uniform in [1e-3, 1]) at a rate the server
+    sustains on one GPU: p50 / p99 latency (submission to completion) and
+    solves per second."""
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    rng = np.random.default_rng(args.seed + 7)
+    images = {n: W.tv_image(100 + i, n=n, polygons=30) for i, n in enumerate(SERVE_SIZES)}
+    S = lf.LatticeServer(workers=workers, max_group=8)
+    for n in SERVE_SIZES:  # engines built and kernels loaded on every worker
+        ts = [S.submit_tv(images[n], 0.01) for _ in range(workers)]
+        for t in ts:
+            S.wait(t)
+            S.release(t)
+    sizes = rng.choice(SERVE_SIZES, size=requests)
+    lams = np.exp(rng.uniform(np.log(1e-3), np.log(1.0), size=requests))
+    arrive = np.cumsum(rng.exponential(1.0 / rate, size=requests))
+    t0 = time.perf_counter()
+    tickets = []
+    for i in range(requests):
+        delay = t0 + arrive[i] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        tickets.append(S.submit_tv(images[int(sizes[i])], float(lams[i])))
+    lat = []
+    for t in tickets:
+        lat.append(S.wait(t))
+        S.release(t)
+    makespan = time.perf_counter() - t0
+    st = S.stats()
+    S.close()
+    lat_ms = np.asarray(lat) * 1e3
+    return {"requests": requests, "rate_per_s": rate, "workers": workers,
+            "sizes": list(SERVE_SIZES), "p50_ms": round(float(np.percentile(lat_ms, 50)), 1),
+            "p99_ms": round(float(np.percentile(lat_ms, 99)), 1),
+            "solves_per_s": round(requests / makespan, 3), "max_in_flight": st["max_in_flight"]}
 
 
 def cpu_baseline(p, budget_s=12.0):
@@ -754,8 +835,9 @@ def parity_check(p, L):
 _W = {}
 
 
-def _ref_init(workload, seed, batch_size=512):
+def _ref_init(workload, seed, batch_size=512, tv_n=256):
     sys.path.insert(0, ROOT)
+    _W["tv_n"] = tv_n
     from oracle import oracle as O
     O.port()
     if workload == "batch":
@@ -763,7 +845,7 @@ def _ref_init(workload, seed, batch_size=512):
         return
     if workload == "tv_path":
         from latticeflow_gb300 import workloads as W
-        _W["tv"] = (W.tv_image(seed, n=TV_PATH_N, polygons=30), tv_path_lambdas())
+        _W["tv"] = (W.tv_image(seed, n=_W.get("tv_n", 256), polygons=30), tv_path_lambdas())
         return
     p = make_workload(workload, seed)
     _W["p"] = p
@@ -774,7 +856,7 @@ def _ref_solve(arg):
     from oracle import oracle as O
     if "tv" in _W:
         f, lams = _W["tv"]
-        _, _, secs = O.port_tv_single("Full2d_4", f, float(lams[arg % len(lams)]))
+        _, secs, _ = O.port_tv_path("Full2d_4", f, lams)
         return secs
     if "batch" in _W:
         secs = 0.0
@@ -805,14 +887,13 @@ def run_reference(args):
     elif args.workload == "tv_path":
         p = None
         per_step = cores
-        # lambdas spread over the path, one per core
-        work = [(c * TV_PATH_LAMBDAS) // cores for c in range(cores)]
+        work = list(range(cores))  # one whole path per core
     else:
         p = make_workload(args.workload, args.seed)
         per_step = cores
         work = list(range(cores))
     with ctx.Pool(cores, initializer=_ref_init,
-                  initargs=(args.workload, args.seed, args.batch_size)) as pool:
+                  initargs=(args.workload, args.seed, args.batch_size, args.tv_n)) as pool:
         for _ in range(args.warmup):
             pool.map(_ref_solve, work, chunksize=1)
         t0 = time.time()
@@ -821,7 +902,7 @@ def run_reference(args):
         wall = time.time() - t0
     value = per_step * args.steps / wall
     kind = "port"
-    unit = "lambda solves/s" if args.workload == "tv_path" else UNIT
+    unit = "paths/s" if args.workload == "tv_path" else UNIT
     out = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": unit,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -831,7 +912,7 @@ def run_reference(args):
         "config": (workload_config(args.workload, p) if p is not None else
                    {"workload": "batch", "lattices": args.batch_size}
                    if args.workload == "batch" else
-                   {"workload": "tv_path", "kernel": "Full2d_4", "shape": [TV_PATH_N, TV_PATH_N],
+                   {"workload": "tv_path", "kernel": "Full2d_4", "shape": [args.tv_n, args.tv_n],
                     "lambdas": "64 values 1e-3*1000^(i/63)", "seed": args.seed}),
         "cpu_baseline": {"value": round(value, 4), "unit": unit, "cores": cores, "kind": kind,
                          "sample": ("each step: one full solve per host core in parallel"
@@ -840,9 +921,8 @@ def run_reference(args):
                                     "each step: all %d lattices spread over the host cores"
                                     " (reference push-relabel restated, oracle/lf_oracle.cpp)"
                                     % args.batch_size if args.workload == "batch" else
-                                    "each step: one single-lambda TV solve per host core, lambdas "
-                                    "spread over the path (reference parametric flow restated, "
-                                    "oracle/lf_oracle.cpp)")},
+                                    "each step: one whole 64-lambda path per host core (the "
+                                    "reference's path tracker restated, oracle/lf_oracle.cpp)")},
         "e2e": {"value": round(value, 4), "unit": unit, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
