@@ -224,6 +224,13 @@ int lf_server_wait(lf_server* s, int64_t ticket, double timeout_s, double* laten
 int lf_server_get_tv(lf_server* s, int64_t ticket, double* out, int64_t* levels);
 int lf_server_get_cut(lf_server* s, int64_t ticket, int* cut, int64_t* flow, int64_t* energy);
 int lf_server_release(lf_server* s, int64_t ticket);
+/* Drop a request that is still queued: its wait then returns LF_ERR_STATE
+ * ("request cancelled").  LF_ERR_STATE if it was admitted already. */
+int lf_server_cancel(lf_server* s, int64_t ticket);
+/* Host-side fault injection: the next `count` engine creations of the
+ * workers fail as a failed device allocation would; the request that needed
+ * the engine finishes with LF_ERR_OOM and the server carries on. */
+int lf_server_inject_alloc_failures(lf_server* s, int count);
 int lf_server_stats(lf_server* s, double* p50_ms, double* p99_ms, double* solves_per_s,
                     int64_t* completed, int64_t* max_in_flight);
 /* max_group = 1 turns grouping off. */

@@ -74,6 +74,8 @@ PROTOTYPES = {
     "lf_server_get_tv": (I, [P, ctypes.c_int64, P, P]),
     "lf_server_get_cut": (I, [P, ctypes.c_int64, P, P, P]),
     "lf_server_release": (I, [P, ctypes.c_int64]),
+    "lf_server_cancel": (I, [P, ctypes.c_int64]),
+    "lf_server_inject_alloc_failures": (I, [P, I]),
     "lf_server_stats": (I, [P, P, P, P, P, P]),
     "lf_server_set_max_group": (I, [P, I]),
     "lf_server_group_stats": (I, [P, P, P]),

@@ -429,6 +429,21 @@ int lf_server_release(lf_server* s, int64_t ticket) {
   });
 }
 
+int lf_server_cancel(lf_server* s, int64_t ticket) {
+  return guarded([&] {
+    if (!s) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    if (!s->s->cancel(ticket))
+      throw lfg::LfError{LF_ERR_STATE, "request already admitted; it cannot be cancelled"};
+  });
+}
+
+int lf_server_inject_alloc_failures(lf_server* s, int count) {
+  return guarded([&] {
+    if (!s) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    s->s->inject_alloc_failures(count);
+  });
+}
+
 int lf_server_stats(lf_server* s, double* p50, double* p99, double* sps, int64_t* completed,
                     int64_t* max_in_flight) {
   return guarded([&] {

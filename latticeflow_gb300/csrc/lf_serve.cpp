@@ -98,6 +98,7 @@ struct Server::Impl {
   Clock::time_point first_submit, last_end;
   bool any = false;
   int device = 0;
+  int fail_allocs = 0;  // engine creations still to fail (host-side fault injection)
 
   bool admissible(const Req& r) const {
     if (in_flight == 0) return true;  // a request larger than the budget runs alone
@@ -187,6 +188,13 @@ struct Server::Impl {
     auto key = std::make_tuple(tv, kd->name, nx, ny, count);
     auto it = w->engines.find(key);
     if (it == w->engines.end()) {
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        if (fail_allocs > 0) {
+          --fail_allocs;
+          throw LfError{5, "device allocation failed (injected)"};
+        }
+      }
       size_t dims[2] = {nx, ny};
       std::unique_ptr<Engine> e(tv ? new_tv_stack_engine(kd, nx, ny, count)
                                    : new Engine("GPUPushRelabel", kd, 2, dims));
@@ -329,6 +337,30 @@ bool Server::wait(int64_t id, double timeout_s, double* latency_s) {
   if (latency_s) *latency_s = std::chrono::duration<double>(r->t_end - r->t_submit).count();
   if (r->status) throw LfError{r->status, r->error};
   return true;
+}
+
+bool Server::cancel(int64_t id) {
+  {
+    std::lock_guard<std::mutex> lk(impl->mu);
+    auto it = impl->reqs.find(id);
+    if (it == impl->reqs.end()) throw LfError{7, "unknown ticket"};
+    auto q = std::find(impl->queue.begin(), impl->queue.end(), it->second);
+    if (q == impl->queue.end()) return false;  // admitted already (or finished)
+    impl->queue.erase(q);
+    Impl::Req& r = *it->second;
+    r.t_start = r.t_end = Clock::now();
+    r.status = 8;
+    r.error = "request cancelled";
+    r.done = true;
+  }
+  impl->cv_done.notify_all();
+  impl->cv_work.notify_all();
+  return true;
+}
+
+void Server::inject_alloc_failures(int n) {
+  std::lock_guard<std::mutex> lk(impl->mu);
+  impl->fail_allocs = std::max(0, n);
 }
 
 namespace {

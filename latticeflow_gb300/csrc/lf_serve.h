@@ -22,6 +22,12 @@ class Server {
   void get_tv(int64_t id, double* out, int64_t* levels);
   void get_cut(int64_t id, int* cut, long long* flow, long long* energy);
   void release(int64_t id);
+  // a request still waiting in the queue is dropped: its wait reports it
+  // cancelled (LF_ERR_STATE); false once it has been admitted
+  bool cancel(int64_t id);
+  // host-side fault injection: the next n engine creations of the workers
+  // fail as a failed device allocation would (the request gets LF_ERR_OOM)
+  void inject_alloc_failures(int n);
   // largest group of same-shape TV requests solved together (1 = none)
   void set_max_group(int g);
   void group_stats(long long* groups, long long* grouped);

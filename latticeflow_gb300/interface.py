@@ -538,6 +538,16 @@ class LatticeServer(object):
         N.check(N.lib().lf_server_release(self._h, ctypes.c_int64(ticket)))
         self._meta.pop(ticket, None)
 
+    def cancel(self, ticket):
+        """Drop a request still waiting in the queue (its wait then raises
+        LF_ERR_STATE); raises LF_ERR_STATE once it has been admitted."""
+        N.check(N.lib().lf_server_cancel(self._h, ctypes.c_int64(ticket)))
+
+    def inject_alloc_failures(self, count):
+        """Fault injection on the host: the next `count` engine creations fail
+        as a failed device allocation would (the request gets LF_ERR_OOM)."""
+        N.check(N.lib().lf_server_inject_alloc_failures(self._h, int(count)))
+
     def stats(self):
         p50, p99, sps = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         c, m = ctypes.c_int64(), ctypes.c_int64()
