@@ -302,7 +302,7 @@ void pool_maps_free(PoolMaps* m) { delete m; }
 int pool2d_tile_rows(const std::vector<InstDesc>& insts) {
   if (insts.size() < 2 || !encode_fn()) return 0;
   const int TB = insts[0].g.TB;
-  if (TB != 8 && TB != 16 && TB != 32) return 0;
+  if (TB != 4 && TB != 8 && TB != 16 && TB != 32) return 0;
   for (const InstDesc& I : insts) {
     if (I.g.TB != TB || I.g.TA != 1 || I.g.A != 1 || I.g.Ap != 1 || I.g.TC != 32) return 0;
     if (I.g.Cp % 32 || I.g.Bp % TB) return 0;
@@ -476,7 +476,7 @@ int lattice2d_kernel_size(const InstDesc& I, bool single) {
   if (!single || !encode_fn()) return 0;
   if (I.g.TA != 1 || I.g.A != 1 || I.g.Ap != 1 || I.g.TC != 32) return 0;
   if (I.node_base != 0 || I.res_base != 0 || I.tile_base != 0 || I.plane != I.g.NP) return 0;
-  if (I.g.TB != 8 && I.g.TB != 16 && I.g.TB != 32) return 0;
+  if (I.g.TB != 4 && I.g.TB != 8 && I.g.TB != 16 && I.g.TB != 32) return 0;
   if (I.g.Cp % 32 || I.g.Bp % I.g.TB) return 0;
   if (stencil_is<4>(I.st)) return 4;
   if (stencil_is<8>(I.st)) return 8;
@@ -497,7 +497,8 @@ cudaError_t launch_pool_pr2d(const PoolPR<int>& p, int K, int variant, unsigned 
     if (variant == 1) return launch_kt<KK, BB, 32>(maps, p, fault, tiles, s);            \
     return launch_kt<KK, BB, 40>(maps, p, fault, tiles, s);                              \
   }
-  LF_PR2D(4, 8) LF_PR2D(4, 16) LF_PR2D(4, 32) LF_PR2D(8, 8) LF_PR2D(8, 16) LF_PR2D(8, 32)
+  LF_PR2D(4, 4) LF_PR2D(4, 8) LF_PR2D(4, 16) LF_PR2D(4, 32) LF_PR2D(8, 4) LF_PR2D(8, 8)
+  LF_PR2D(8, 16) LF_PR2D(8, 32)
 #undef LF_PR2D
   return cudaErrorInvalidValue;
 }
@@ -560,7 +561,8 @@ cudaError_t loop_pool_pr2d(PassLoop* L, const PoolPR<int>& p, int K, int variant
     if (variant == 1) return loop_kt<KK, BB, 32>(L, maps, p, fault, tiles, ctl, cap, passes, s); \
     return loop_kt<KK, BB, 40>(L, maps, p, fault, tiles, ctl, cap, passes, s);                  \
   }
-  LF_PR2D(4, 8) LF_PR2D(4, 16) LF_PR2D(4, 32) LF_PR2D(8, 8) LF_PR2D(8, 16) LF_PR2D(8, 32)
+  LF_PR2D(4, 4) LF_PR2D(4, 8) LF_PR2D(4, 16) LF_PR2D(4, 32) LF_PR2D(8, 4) LF_PR2D(8, 8)
+  LF_PR2D(8, 16) LF_PR2D(8, 32)
 #undef LF_PR2D
   return cudaErrorInvalidValue;
 }
@@ -574,7 +576,8 @@ cudaError_t loop_pool_bfs2d(PassLoop* L, const PoolBFS& p, int K, unsigned long 
 #define LF_BFS2D(KK, BB)                                                                      \
   if (K == KK && TB == BB)                                                                      \
     return bfs_loop_kt<KK, BB>(L, maps, p, fault, tiles, ctl, cap, passes, overflow, s);
-  LF_BFS2D(4, 8) LF_BFS2D(4, 16) LF_BFS2D(4, 32) LF_BFS2D(8, 8) LF_BFS2D(8, 16) LF_BFS2D(8, 32)
+  LF_BFS2D(4, 4) LF_BFS2D(4, 8) LF_BFS2D(4, 16) LF_BFS2D(4, 32) LF_BFS2D(8, 4) LF_BFS2D(8, 8)
+  LF_BFS2D(8, 16) LF_BFS2D(8, 32)
 #undef LF_BFS2D
   return cudaErrorInvalidValue;
 }
@@ -598,7 +601,8 @@ cudaError_t pr2d64(PassLoop* L, const PoolPR<long long>& p, int K, unsigned long
     kern = kt64_setup<KK, BB>(grid);                    \
     smem = PR2dLayout64<KK, BB>::smem_bytes;            \
   }
-  LF_P64(4, 8) LF_P64(4, 16) LF_P64(4, 32) LF_P64(8, 8) LF_P64(8, 16) LF_P64(8, 32)
+  LF_P64(4, 4) LF_P64(4, 8) LF_P64(4, 16) LF_P64(4, 32) LF_P64(8, 4) LF_P64(8, 8)
+  LF_P64(8, 16) LF_P64(8, 32)
 #undef LF_P64
   if (!kern) return cudaErrorInvalidValue;
   grid = std::max(1, std::min(grid, tiles));
@@ -632,7 +636,7 @@ cudaError_t pool_pr2d(PassLoop* L, const void* maps, const PoolPR<int>& p, int T
     kern = variant == 1 ? kt_pool_setup<BB, 32>(grid) : kt_pool_setup<BB, 40>(grid); \
     smem = PR2dPoolLayout<BB>::smem_bytes;                                           \
   }
-  LF_PP(8) LF_PP(16) LF_PP(32)
+  LF_PP(4) LF_PP(8) LF_PP(16) LF_PP(32)
 #undef LF_PP
   if (!kern) return cudaErrorInvalidValue;
   grid = std::max(1, std::min(grid, tiles));
@@ -669,7 +673,7 @@ cudaError_t pool_bfs2d(PassLoop* L, const void* maps, const PoolBFS& p, int TB,
     kern = bfs_kt_pool_setup<BB>(grid);        \
     smem = BFS2dLayout<BB>::smem_bytes;        \
   }
-  LF_PB(8) LF_PB(16) LF_PB(32)
+  LF_PB(4) LF_PB(8) LF_PB(16) LF_PB(32)
 #undef LF_PB
   if (!kern) return cudaErrorInvalidValue;
   grid = std::max(1, std::min(grid, tiles));
@@ -702,7 +706,8 @@ cudaError_t launch_pool_bfs2d(const PoolBFS& p, int K, unsigned long long* fault
   if (!bfs_maps_for(p, TB, maps)) return cudaErrorInvalidValue;
 #define LF_BFS2D(KK, BB) \
   if (K == KK && TB == BB) return launch_bfs_kt<KK, BB>(maps, p, fault, tiles, s);
-  LF_BFS2D(4, 8) LF_BFS2D(4, 16) LF_BFS2D(4, 32) LF_BFS2D(8, 8) LF_BFS2D(8, 16) LF_BFS2D(8, 32)
+  LF_BFS2D(4, 4) LF_BFS2D(4, 8) LF_BFS2D(4, 16) LF_BFS2D(4, 32) LF_BFS2D(8, 4) LF_BFS2D(8, 8)
+  LF_BFS2D(8, 16) LF_BFS2D(8, 32)
 #undef LF_BFS2D
   return cudaErrorInvalidValue;
 }

@@ -91,7 +91,7 @@ def test_batch_3d_and_errors(native, gpu, oracle_port):
 
 
 @pytest.mark.parametrize("pr_kernel,bfs_kernel,device_loops", [(0, 0, 1), (0, 0, 0), (1, 1, 0), (2, 0, 1)])
-@pytest.mark.parametrize("tile_rows", [8, 16, 32])
+@pytest.mark.parametrize("tile_rows", [4, 8, 16, 32])
 def test_batch_pass_variants(native, gpu, oracle_port, pr_kernel, bfs_kernel, device_loops, tile_rows):
     """A pool of mixed 4- and 8-connected lattices through the TMA-staged pool
     passes (device-side loops or one launch per pass) and the generic tile

@@ -148,7 +148,7 @@ def test_level_reductions_vs_oracle(native, gpu, oracle_port, kernel, dims):
 
 @pytest.mark.parametrize("kernel,dims", [("Full2d_4", (70, 66)), ("Full2d_8", (45, 52))])
 @pytest.mark.parametrize("pr_kernel,device_loops,tile_rows", [(0, 1, 8), (0, 1, 16), (0, 0, 32),
-                                                              (1, 1, 16), (1, 0, 32)])
+                                                              (1, 1, 16), (1, 0, 32), (0, 0, 4)])
 def test_level_reductions_pass_variants(native, gpu, oracle_port, kernel, dims, pr_kernel,
                                         device_loops, tile_rows):
     """Section solves through the TMA-staged 64-bit pass with section masks
