@@ -160,7 +160,8 @@ int lf_set_tuning(lf_lattice* h, int tile_rows, int local_sweeps, int launches_p
  * solve gives up with LF_ERR_NO_CONVERGENCE; 0 = 1,000,000; the handle stays
  * usable), "pr_kernel" (push/relabel pass of 2-d 3x3 lattices: 0 = staged by
  * bulk tensor copies, 40 registers; 1 = generic tile kernel; 2 = staged, 32
- * registers), "bfs_kernel" (global-relabel pass of those lattices: 0 =
+ * registers; 3 = staged, one warp per tile, launched one pass at a time),
+ * "bfs_kernel" (global-relabel pass of those lattices: 0 =
  * staged, 1 = generic), "device_loops" (1 = the staged passes of a relabel or
  * an epoch run as one CUDA graph with a device-side loop; 0 = one launch per
  * pass, the default), "fill_kernel" (energy fill of device-resident arrays:

@@ -16,6 +16,7 @@ import math
 import os
 
 DEFAULT_GRID = {
+    "pr_kernel": (0, 3),
     "tile_rows": (4, 8, 16, 32),
     "local_sweeps": (1, 2, 4),
     "launches_per_relabel": (4, 8, 16),

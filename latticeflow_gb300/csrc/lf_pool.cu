@@ -34,9 +34,10 @@ namespace {
 
 inline int nblk(long long n, int t) { return int((n + t - 1) / t); }
 
-// tuning value pr_kernel -> variant of the TMA-staged push/relabel pass
+// tuning value pr_kernel -> variant of the TMA-staged push/relabel pass:
+// 0 block per tile (40 registers), 1 the same with 32, 2 warp per tile
 inline int pr2d_variant(int pr_kernel) {
-  return pr_kernel == 2 ? 1 : 0;
+  return pr_kernel == 2 ? 1 : pr_kernel == 3 ? 2 : 0;
 }
 
 // lattice of pool node i (node_base ascending, n entries + sentinel)

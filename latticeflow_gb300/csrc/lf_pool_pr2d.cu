@@ -113,6 +113,42 @@ cudaError_t launch_kt(const PR2dMaps& maps, const PoolPR<int>& p, unsigned long 
   return cudaGetLastError();
 }
 
+// The warp-per-tile variant: 4 warps per block, each with its own stage
+// buffers.
+constexpr int kPr2dWarps = 4;
+
+template <int K, int TB>
+size_t kt_warp_smem() {
+  return size_t(kPr2dWarps) * PR2dWarpLayout<K, TB>::per_warp + 128;
+}
+
+template <int K, int TB>
+void* kt_warp_setup(int& grid) {
+  auto kern = k_pool_pr2d_warp<K, TB, kPr2dWarps>;
+  static std::mutex mu;
+  static int cap = 0;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!cap) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(kt_warp_smem<K, TB>()));
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cap = occupancy_grid(kern, kPr2dWarps * 32, kt_warp_smem<K, TB>());
+  }
+  grid = cap;
+  return reinterpret_cast<void*>(kern);
+}
+
+template <int K, int TB>
+cudaError_t launch_kt_warp(const PR2dMaps& maps, const PoolPR<int>& p, unsigned long long* fault,
+                           int tiles, cudaStream_t s) {
+  int grid = 0;
+  kt_warp_setup<K, TB>(grid);
+  const int need = (tiles + kPr2dWarps - 1) / kPr2dWarps;
+  k_pool_pr2d_warp<K, TB, kPr2dWarps><<<std::max(1, std::min(grid, need)), kPr2dWarps * 32,
+                                        kt_warp_smem<K, TB>(), s>>>(maps, p, fault);
+  return cudaGetLastError();
+}
+
 // Tensor maps of the 64-bit pass with section masks, cached per host thread.
 struct MapCache64 {
   const void *res = nullptr, *exc = nullptr, *h = nullptr, *km = nullptr;
@@ -495,6 +531,7 @@ cudaError_t launch_pool_pr2d(const PoolPR<int>& p, int K, int variant, unsigned 
 #define LF_PR2D(KK, BB)                                                                \
   if (K == KK && TB == BB) {                                                             \
     if (variant == 1) return launch_kt<KK, BB, 32>(maps, p, fault, tiles, s);            \
+    if (variant == 2 && BB <= 8) return launch_kt_warp<KK, (BB <= 8 ? BB : 8)>(maps, p, fault, tiles, s); \
     return launch_kt<KK, BB, 40>(maps, p, fault, tiles, s);                              \
   }
   LF_PR2D(4, 4) LF_PR2D(4, 8) LF_PR2D(4, 16) LF_PR2D(4, 32) LF_PR2D(8, 4) LF_PR2D(8, 8)

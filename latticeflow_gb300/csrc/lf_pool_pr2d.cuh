@@ -418,6 +418,212 @@ __global__ void __maxnreg__(REGS)
   }
 }
 
+// ------------------------------------------------ one warp per tile
+//
+// The same pass with a whole tile per warp: lane c owns column c of the tile
+// (TB nodes, one per row), the phases of a sweep are separated by warp
+// syncs instead of block barriers, and the warps of a block work on
+// different tiles, each with its own two stage buffers and mbarriers.  A
+// warp's stalls then hold up only its own tile.  Pushes inside the tile go
+// to nodes of the same lane (vertical) or of the lanes beside it, by
+// shared-memory atomics on the excess; as in pr2d_tile, a push from j to a
+// lower neighbour is the only write of that neighbour's reverse residual in
+// the phase (the neighbour pushes only further down).
+
+template <int K, int TB>
+struct PR2dWarpLayout {
+  using Ly = PR2dLayout<K, TB>;
+  // two stage buffers, then two mbarriers (8 bytes each); 128-aligned
+  static constexpr int per_warp = (2 * Ly::stage_bytes + 16 + 127) / 128 * 128;
+};
+
+template <int K, int TB>
+__device__ __forceinline__ void pr2d_tile_warp(const PoolPR<int>& p, const Geo& g, int hmax,
+                                               int cur, int* s_res, int* s_exc, int* s_h,
+                                               int tile, const int* e0) {
+  constexpr int NT = TB * 32;
+  constexpr int HW = kPr2dHaloW;
+  constexpr int half = K / 2;
+  const int lane = threadIdx.x & 31;
+  const int tc = tile % g.ntc, tb = tile / g.ntc;
+  const int b0 = tb * TB, c0 = tc * 32;
+  const int nxt = cur ^ 1;
+  unsigned nbr = 0;  // neighbour tiles this lane's pushes reached
+  // a node's own height sits in its staged slot: only its lane writes it
+  for (int it = 0; it < p.sweeps; ++it) {
+    // push phase (heights frozen)
+#pragma unroll 1
+    for (int r = 0; r < TB; ++r) {
+      const int t = r * 32 + lane;
+      const int e = s_exc[t];
+      if (e <= 0) continue;
+      const int hidx = (r + 1) * HW + (lane + 4);
+      const int hr = s_h[hidx];
+      int sent = 0;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int rem = e - sent;
+        if (rem <= 0) break;
+        const int rv = s_res[k * NT + t];
+        if (rv <= 0) continue;
+        if (s_h[hidx + s2_db<K>(k) * HW + s2_dc<K>(k)] >= hr) continue;
+        const int d = rem < rv ? rem : rv;
+        s_res[k * NT + t] = rv - d;
+        sent += d;
+        const int rk = k < half ? k + half : k - half;
+        const int nb = r + s2_db<K>(k), nc = lane + s2_dc<K>(k);
+        if (nb >= 0 && nb < TB && nc >= 0 && nc < 32) {
+          const int tn = nb * 32 + nc;
+          atomicAdd(&s_exc[tn], d);
+          s_res[rk * NT + tn] += d;
+        } else {
+          // across the tile edge: delivered at once with global atomics
+          const long long gi = (long long)(b0 + r) * g.Cp + (c0 + lane);
+          const long long dn = (long long)s2_db<K>(k) * g.Cp + s2_dc<K>(k);
+          atomicAdd(p.res + (long long)k * g.NP + gi, -d);
+          atomicAdd(p.res + (long long)rk * g.NP + gi + dn, d);
+          atomicAdd(p.exc + gi + dn, d);
+          const int dtb = nb < 0 ? -1 : nb >= TB ? 1 : 0;
+          const int dtc = nc < 0 ? -1 : nc >= 32 ? 1 : 0;
+          nbr |= nbr_bit(dtb, dtc);
+        }
+      }
+      if (sent) atomicAdd(&s_exc[t], -sent);
+    }
+    __syncwarp();
+    // relabel phase
+    int act = 0;
+#pragma unroll 1
+    for (int r = 0; r < TB; ++r) {
+      const int t = r * 32 + lane;
+      const int hidx = (r + 1) * HW + (lane + 4);
+      int hr = s_h[hidx];
+      if (s_exc[t] <= 0 || hr >= hmax) continue;
+      int hmin = kHInf;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        if (s_res[k * NT + t] > 0) {
+          const int hn = s_h[hidx + s2_db<K>(k) * HW + s2_dc<K>(k)];
+          hmin = hn < hmin ? hn : hmin;
+        }
+      }
+      if (hmin >= hr) {
+        hr = (hmin >= hmax - 1) ? hmax : hmin + 1;
+        s_h[hidx] = hr;
+      }
+      act |= hr < hmax;
+    }
+    __syncwarp();
+    if (it + 1 == p.sweeps) break;
+    if (!__any_sync(0xffffffffu, act)) break;
+  }
+  // write-back: interior excess and residuals as staged, edge excess as a
+  // delta (other tiles' pushes arrive there by atomics), heights
+  int still = 0;
+#pragma unroll
+  for (int r = 0; r < TB; ++r) {
+    const int t = r * 32 + lane;
+    const long long gi = (long long)(b0 + r) * g.Cp + (c0 + lane);
+    const int ef = s_exc[t];
+    const int hr = s_h[(r + 1) * HW + (lane + 4)];
+    const bool edge = r == 0 || r == TB - 1 || lane == 0 || lane == 31;
+    if (edge) atomicAdd(p.exc + gi, ef - e0[r]);
+    else p.exc[gi] = ef;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int nb = r + s2_db<K>(k), nc = lane + s2_dc<K>(k);
+      if (nb >= 0 && nb < TB && nc >= 0 && nc < 32) p.res[(long long)k * g.NP + gi] = s_res[k * NT + t];
+    }
+    p.h[gi] = hr;
+    still |= ef > 0 && hr < hmax;
+  }
+  nbr = __reduce_or_sync(0xffffffffu, nbr);
+  const bool again = __any_sync(0xffffffffu, still);
+  // the buffer's next contents come from the async proxy: order this
+  // visit's shared-memory accesses before them
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncwarp();
+  if (lane < 8 && ((nbr >> lane) & 1u)) {
+    const int dtb = (lane == 0 || lane == 4 || lane == 5) ? -1 : (lane == 1 || lane == 6 || lane == 7) ? 1 : 0;
+    const int dtc = (lane == 2 || lane == 4 || lane == 6) ? -1 : (lane == 3 || lane == 5 || lane == 7) ? 1 : 0;
+    // a bit is set only by a push, which never leaves the lattice
+    enqueue_tile(p.q, nxt, tile + dtb * g.ntc + dtc);
+  }
+  if (again && lane == 0) enqueue_tile(p.q, nxt, tile);
+}
+
+// One lattice (the pool of one), 32-bit capacities, no section mask; W
+// warps per block, each taking the queued tiles gw, gw + warps, ... in turn.
+template <int K, int TB, int W>
+__global__ void __launch_bounds__(W * 32)
+    k_pool_pr2d_warp(const __grid_constant__ PR2dMaps maps, PoolPR<int> p,
+                     unsigned long long* fault) {
+  using Ly = PR2dLayout<K, TB>;
+  using WL = PR2dWarpLayout<K, TB>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<unsigned long long>(smem_raw) + 127) & ~127ull);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char* mine = smem + warp * WL::per_warp;
+  const unsigned stage0 = smem_addr(mine);
+  const unsigned bar0 = smem_addr(mine + 2 * Ly::stage_bytes);
+  const Geo& g = p.inst0.g;
+  const int cur = p.cur;
+  const unsigned n = queued_count(p.q, cur);
+  const int* list = p.q.list[cur];
+  const unsigned gw = blockIdx.x * W + warp, nw = gridDim.x * W;
+  if (gw >= n) return;  // the whole warp: no block barrier follows
+  const int hmax = p.inst0.hmax;
+  const bool done = p.inst0.done != 0;
+  if (lane == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar0 + 8, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  if (lane == 0 && !done) pr2d_issue<K, TB>(maps, g, list[gw], stage0, bar0);
+  unsigned phases = 0, buf = 0;
+  for (unsigned i = gw; i < n; i += nw, buf ^= 1) {
+    const int gt = list[i];
+    if (lane == 0) {
+      p.q.flag[cur][gt] = 0;
+      atomicAdd(&p.counters[0], 1ull);
+    }
+    if (done) continue;
+    const unsigned nx = i + nw;
+    if (lane == 0 && nx < n)
+      pr2d_issue<K, TB>(maps, g, list[nx], stage0 + (buf ^ 1) * Ly::stage_bytes,
+                        bar0 + (buf ^ 1) * 8);
+    const unsigned bar = bar0 + buf * 8;
+    const unsigned par = (phases >> buf) & 1u;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(bar, par, kPr2dWaitLimit));
+    phases ^= 1u << buf;
+    if (!ok) {
+      // a copy did not land: record it, wait (bounded) for the copies still
+      // in flight so that none lands after the warp is gone, and stop
+      if (lane == 0) atomicExch(fault, 1ull);
+      mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+      if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
+      return;
+    }
+    if (!tile_ok(gt, g.ntiles)) {
+      if (lane == 0) atomicExch(fault, 2ull);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      continue;
+    }
+    unsigned char* st = mine + buf * Ly::stage_bytes;
+    int* s_res = reinterpret_cast<int*>(st);
+    int* s_exc = reinterpret_cast<int*>(st + Ly::res_bytes);
+    int* s_h = reinterpret_cast<int*>(st + Ly::res_bytes + Ly::exc_bytes);
+    int e0[TB];
+#pragma unroll
+    for (int r = 0; r < TB; ++r) e0[r] = s_exc[r * 32 + lane];
+    __syncwarp();  // every lane has read its staged excess before any push
+    pr2d_tile_warp<K, TB>(p, g, hmax, cur, s_res, s_exc, s_h, gt, e0);
+  }
+}
+
 // ------------------------------------------------ 64-bit, section mask
 
 // tensor maps of one lattice for the 64-bit pass: residual planes, excess

@@ -26,7 +26,8 @@ struct Tuning {
   int tail_tree_nodes = 0;       // nodes of one tail-step tree at most; 0 = 65,536
   int pr_kernel = 0;             // push/relabel pass of a plain 2-d cut: 0 = TMA-staged
                                  // (40 registers), 1 = generic tile kernel, 2 = TMA-staged
-                                 // with 32 registers
+                                 // with 32 registers, 3 = TMA-staged, one warp per tile
+                                 // (one launch per pass)
   int bfs_kernel = 0;            // BFS pass of a single 2-d lattice: 0 = TMA-staged,
                                  // 1 = generic tile kernel
   int device_loops = 0;          // TMA-staged passes: 1 = device-side pass loops (CUDA

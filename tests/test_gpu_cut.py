@@ -225,14 +225,15 @@ def test_pinned_host_arrays_read_in_place(native, gpu):
 
 
 @pytest.mark.parametrize("pr_kernel,bfs_kernel,device_loops", [(0, 0, 1), (0, 0, 0), (1, 1, 1), (2, 0, 1),
-                                                                (1, 0, 1), (0, 1, 1)])
+                                                                (1, 0, 1), (0, 1, 1), (3, 0, 0),
+                                                                (3, 1, 0)])
 @pytest.mark.parametrize("kernel,dims,tile_rows", [
     ("Full2d_8", (200, 230), 8), ("Full2d_8", (256, 160), 16), ("Full2d_8", (97, 300), 32),
     ("Full2d_4", (210, 190), 16), ("Full2d_4", (64, 500), 32), ("Full2d_8", (150, 170), 4),
     ("Full2d_4", (130, 99), 4)], ids=lambda v: str(v))
 def test_push_relabel_kernels_agree(native, gpu, oracle_port, pr_kernel, bfs_kernel, device_loops,
                                     kernel, dims, tile_rows):
-    """The TMA-staged 2-d passes (pr_kernel 0, 2; bfs_kernel 0), in
+    """The TMA-staged 2-d passes (pr_kernel 0, 2, 3; bfs_kernel 0), in
     device-side loops (device_loops 1) or launched one by one (0), and the
     generic tile passes (1) give the reference's exact answer at every tile
     height."""
@@ -279,7 +280,7 @@ def test_tma_pass_full_size_all_variants(native, gpu, oracle_port):
     u, b = p.energies()
     ref = None
     for prk, rows, dl in ((1, 16, 0), (0, 16, 1), (0, 16, 0), (2, 16, 1), (0, 8, 1), (2, 8, 0),
-                          (0, 32, 1), (2, 32, 0), (0, 4, 0), (2, 4, 0)):
+                          (0, 32, 1), (2, 32, 0), (0, 4, 0), (2, 4, 0), (3, 4, 0), (3, 8, 0)):
         L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
         L.setParam("pr_kernel", prk)
         L.setParam("bfs_kernel", 1 if ref is None else 0)  # the reference run: generic passes
