@@ -188,6 +188,18 @@ int lf_batch_add_energy_potentials(lf_batch* b, int index, const int64_t* unary,
                                    const int64_t* binary);
 int lf_batch_add_capacities(lf_batch* b, int index, const int32_t* source, const int32_t* sink,
                             const int32_t* edge);
+/* Every lattice's capacities at once: source / sink hold all lattices' nodes
+ * back to back in index order (sum of N_i ints each), edge all lattices'
+ * filling edges (sum of N_i * K_i/2 ints); any pointer may be NULL.  One
+ * copy per array instead of one call per lattice.  Accumulates. */
+int lf_batch_add_capacities_packed(lf_batch* b, const int32_t* source, const int32_t* sink,
+                                   const int32_t* edge);
+/* Every lattice's minimal (maximal = 0) or maximal (maximal = 1) on-set,
+ * back to back in index order (sum of N_i ints). */
+int lf_batch_get_cuts_packed(lf_batch* b, int* cuts_out, int maximal);
+/* Every lattice's flow value and minimum energy (lf_batch_size entries each;
+ * either pointer may be NULL). */
+int lf_batch_get_flows(lf_batch* b, int64_t* flows, int64_t* energies);
 int lf_batch_clear(lf_batch* b);
 int lf_batch_run(lf_batch* b);
 double lf_batch_run_time(const lf_batch* b);

@@ -57,6 +57,9 @@ PROTOTYPES = {
     "lf_batch_size": (I, [P]),
     "lf_batch_add_energy_potentials": (I, [P, I, P, P]),
     "lf_batch_add_capacities": (I, [P, I, P, P, P]),
+    "lf_batch_add_capacities_packed": (I, [P, P, P, P]),
+    "lf_batch_get_cuts_packed": (I, [P, P, I]),
+    "lf_batch_get_flows": (I, [P, P, P]),
     "lf_batch_clear": (I, [P]),
     "lf_batch_run": (I, [P]),
     "lf_batch_run_time": (ctypes.c_double, [P]),

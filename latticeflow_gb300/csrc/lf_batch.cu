@@ -141,6 +141,37 @@ void Batch::add_caps(int i, const int32_t* src, const int32_t* snk, const int32_
   if (!defer_checks) check_err("capacities must be non-negative");
 }
 
+// Every lattice's capacities from three packed host arrays (lattices back to
+// back in index order): one copy per array, then the fill kernels.
+void Batch::add_caps_packed(const int32_t* src, const int32_t* snk, const int32_t* edge) {
+  alloc_accumulators();
+  long long nodes = 0, edges = 0;
+  for (const Member& m : members) {
+    nodes += m.N;
+    edges += m.N * (m.st.K / 2);
+  }
+  DevBuf<int32_t> stage;
+  stage.alloc(size_t(2 * nodes + edges) + 1, stream);
+  int32_t* ds = src ? stage.p : nullptr;
+  int32_t* dt = snk ? stage.p + nodes : nullptr;
+  int32_t* de = edge ? stage.p + 2 * nodes : nullptr;
+  if (src) check(cudaMemcpyAsync(ds, src, nodes * 4, cudaMemcpyHostToDevice, stream), "memcpy");
+  if (snk) check(cudaMemcpyAsync(dt, snk, nodes * 4, cudaMemcpyHostToDevice, stream), "memcpy");
+  if (edge) check(cudaMemcpyAsync(de, edge, edges * 4, cudaMemcpyHostToDevice, stream), "memcpy");
+  long long no = 0, eo = 0;
+  for (size_t i = 0; i < members.size(); ++i) {
+    Member& m = members[i];
+    check(launch_fill_caps(m.g, m.st, m.nd, m.N, ds ? ds + no : nullptr, dt ? dt + no : nullptr,
+                           de ? de + eo : nullptr, d_exc64 + m.node_base, d_cap64 + m.res_base,
+                           d_c0 + i, d_err, 0, stream),
+          "fill caps");
+    no += m.N;
+    eo += m.N * (m.st.K / 2);
+  }
+  solved = false;
+  if (!defer_checks) check_err("capacities must be non-negative");
+}
+
 void Batch::add_energy(int i, const int64_t* unary, const int64_t* binary) {
   alloc_accumulators();
   Member& m = member(i);
@@ -268,6 +299,13 @@ void Batch::fetch_cuts() {
   }
   cut_total = total;
   cuts_fetched = true;
+}
+
+// Every lattice's cut, back to back in index order.
+void Batch::get_cuts_packed(int* out, bool maximal) {
+  if (!solved) throw LfError{8, "getCut called before run"};
+  fetch_cuts();
+  std::memcpy(out, host_cuts.data() + (maximal ? cut_total : 0), cut_total * sizeof(int));
 }
 
 void Batch::get_cut(int i, int* out, bool maximal) {

@@ -30,6 +30,8 @@ class Batch {
   int add(const KernelDef* kd, int nd, const size_t* dims);
   void add_caps(int i, const int32_t* src, const int32_t* snk, const int32_t* edge);
   void add_energy(int i, const int64_t* unary, const int64_t* binary);
+  void add_caps_packed(const int32_t* src, const int32_t* snk, const int32_t* edge);
+  void get_cuts_packed(int* out, bool maximal);
   void clear();
   void run();
   void get_cut(int i, int* out, bool maximal);

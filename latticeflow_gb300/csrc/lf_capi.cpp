@@ -535,6 +535,32 @@ int lf_batch_add_capacities(lf_batch* b, int index, const int32_t* src, const in
   });
 }
 
+int lf_batch_add_capacities_packed(lf_batch* b, const int32_t* src, const int32_t* snk,
+                                   const int32_t* edge) {
+  return guarded([&] {
+    if (!b) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    b->b->add_caps_packed(src, snk, edge);
+  });
+}
+
+int lf_batch_get_cuts_packed(lf_batch* b, int* cuts_out, int maximal) {
+  return guarded([&] {
+    if (!b || !cuts_out) throw lfg::LfError{LF_ERR_INVALID, "null argument"};
+    b->b->get_cuts_packed(cuts_out, maximal != 0);
+  });
+}
+
+int lf_batch_get_flows(lf_batch* b, int64_t* flows, int64_t* energies) {
+  return guarded([&] {
+    if (!b) throw lfg::LfError{LF_ERR_INVALID, "null handle"};
+    if (!b->b->solved) throw lfg::LfError{LF_ERR_STATE, "flows are available after run"};
+    for (size_t i = 0; i < b->b->members.size(); ++i) {
+      if (flows) flows[i] = b->b->members[i].flow;
+      if (energies) energies[i] = b->b->members[i].energy;
+    }
+  });
+}
+
 int lf_batch_clear(lf_batch* b) {
   return guarded([&] {
     if (!b) throw lfg::LfError{LF_ERR_INVALID, "null handle"};

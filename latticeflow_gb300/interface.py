@@ -420,6 +420,42 @@ class LatticeBatch(object):
         N.check(N.lib().lf_batch_add_capacities(
             self._h, index, *[(_p(a) if a is not None else None) for a in arrs]))
 
+    def addCapacitiesPacked(self, source=None, sink=None, edges=None):
+        """Every lattice's capacities in one call: source / sink with all
+        lattices' nodes back to back in index order, edges all lattices'
+        filling edges back to back (lf_batch_add_capacities_packed)."""
+        n = sum(int(np.prod(s)) for s in self._shapes)
+        ne = sum(int(np.prod(s)) * e for s, e in zip(self._shapes, self._edges))
+        arrs = []
+        for a, m in ((source, n), (sink, n), (edges, ne)):
+            if a is None:
+                arrs.append(None)
+                continue
+            a = np.ascontiguousarray(a, dtype=np.int32).reshape(-1)
+            if a.size != m:
+                raise ValueError("packed capacity array has the wrong size")
+            arrs.append(a)
+        N.check(N.lib().lf_batch_add_capacities_packed(
+            self._h, *[(_p(a) if a is not None else None) for a in arrs]))
+
+    def getCutsPacked(self, maximal=False, out=None):
+        """Every lattice's cut back to back in index order (one flat int32
+        array; lf_batch_get_cuts_packed)."""
+        n = sum(int(np.prod(s)) for s in self._shapes)
+        if out is None:
+            out = np.empty(n, dtype=np.int32)
+        elif out.dtype != np.int32 or out.size != n or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous int32 array of the batch's node count")
+        N.check(N.lib().lf_batch_get_cuts_packed(self._h, _p(out), 1 if maximal else 0))
+        return out
+
+    def flows(self):
+        """(flow values, minimum energies) of every lattice, int64 arrays."""
+        f = np.empty(len(self._shapes), dtype=np.int64)
+        e = np.empty(len(self._shapes), dtype=np.int64)
+        N.check(N.lib().lf_batch_get_flows(self._h, _p(f), _p(e)))
+        return f, e
+
     def addEnergyPotentials(self, index, unary, binary):
         n = int(np.prod(self._shapes[index]))
         u = np.ascontiguousarray(unary, dtype=np.int64).reshape(-1)
@@ -452,14 +488,6 @@ class LatticeBatch(object):
         e = ctypes.c_int64(0)
         N.check(N.lib().lf_batch_get_flow(self._h, index, ctypes.byref(f), ctypes.byref(e)))
         return f.value, e.value
-
-    def levelSets(self):
-        """Parametric solver: the level set of every node, numbered in the
-        order ParametricFlowSolver::run returns the level sets
-        (parametricflow/pf_solver.hpp:180-203)."""
-        out = np.empty(self.n_nodes, dtype=np.int32)
-        N.check(N.lib().lf_get_level_sets(self._h, _p(out)))
-        return out.reshape(self._dimensions)
 
     def stats(self):
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

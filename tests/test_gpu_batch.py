@@ -119,3 +119,33 @@ def test_batch_pass_variants(native, gpu, oracle_port, pr_kernel, bfs_kernel, de
             assert B.flow(i)[1] == E, (rep, i)
             assert np.array_equal(B.getCut(i), cmin), (rep, i)
             assert np.array_equal(B.getCutMax(i), cmax), (rep, i)
+
+
+def test_batch_packed_fill_and_results(native, gpu, oracle_port):
+    """The packed calls (one fill for every lattice, every cut in one array)
+    give the per-lattice calls' results and the oracle's."""
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    shapes = W.batch_shapes(20, seed=8, lo=20, hi=160)
+    probs = [W.plain_cut(700 + i, s, "Full2d_4" if i % 2 else "Full2d_8") for i, s in enumerate(shapes)]
+    B = lf.LatticeBatch()
+    for p in probs:
+        B.add(p.kernel, p.dims)
+    B.addCapacitiesPacked(np.concatenate([p.source for p in probs]),
+                          np.concatenate([p.sink for p in probs]),
+                          np.concatenate([p.edge.reshape(-1) for p in probs]))
+    B.run()
+    cuts = B.getCutsPacked()
+    cuts_max = B.getCutsPacked(maximal=True)
+    flows, energies = B.flows()
+    off = 0
+    for i, p in enumerate(probs):
+        u, b = p.energies()
+        E, cmin, cmax, _, _ = oracle_port.port_canonical(p.kernel, p.dims, u, b)
+        assert energies[i] == E and B.flow(i) == (flows[i], energies[i])
+        assert np.array_equal(cuts[off:off + p.n].reshape(p.dims), cmin)
+        assert np.array_equal(cuts_max[off:off + p.n].reshape(p.dims), cmax)
+        assert np.array_equal(B.getCut(i), cmin)
+        off += p.n
+    with pytest.raises(ValueError):
+        B.addCapacitiesPacked(np.zeros(3, dtype=np.int32))
