@@ -302,10 +302,28 @@ void Batch::fetch_cuts() {
 }
 
 // Every lattice's cut, back to back in index order.
+// The requested set only, extracted on the device and copied straight into
+// the caller's buffer (pinned memory makes it one DMA).
 void Batch::get_cuts_packed(int* out, bool maximal) {
   if (!solved) throw LfError{8, "getCut called before run"};
-  fetch_cuts();
-  std::memcpy(out, host_cuts.data() + (maximal ? cut_total : 0), cut_total * sizeof(int));
+  if (cuts_fetched) {
+    std::memcpy(out, host_cuts.data() + (maximal ? cut_total : 0), cut_total * sizeof(int));
+    return;
+  }
+  long long total = 0;
+  for (Member& m : members) total += m.N;
+  DevBuf<int> stage;
+  stage.alloc(std::max<long long>(total, 1), stream);
+  long long off = 0;
+  for (Member& m : members) {
+    check(launch_extract_cuts(m.g, m.nd, m.N, d_mark + m.node_base, d_h + m.node_base,
+                              maximal ? nullptr : stage.p + off, maximal ? stage.p + off : nullptr,
+                              stream),
+          "extract cuts");
+    off += m.N;
+  }
+  check(cudaMemcpyAsync(out, stage.p, total * sizeof(int), cudaMemcpyDeviceToHost, stream), "memcpy");
+  check(cudaStreamSynchronize(stream), "sync");
 }
 
 void Batch::get_cut(int i, int* out, bool maximal) {
