@@ -150,14 +150,38 @@ void Batch::add_caps_packed(const int32_t* src, const int32_t* snk, const int32_
     nodes += m.N;
     edges += m.N * (m.st.K / 2);
   }
+  // pinned caller arrays are read in place by the fill kernels (the transfer
+  // overlaps the fills); pageable ones are copied to a staging buffer first
   DevBuf<int32_t> stage;
-  stage.alloc(size_t(2 * nodes + edges) + 1, stream);
-  int32_t* ds = src ? stage.p : nullptr;
-  int32_t* dt = snk ? stage.p + nodes : nullptr;
-  int32_t* de = edge ? stage.p + 2 * nodes : nullptr;
-  if (src) check(cudaMemcpyAsync(ds, src, nodes * 4, cudaMemcpyHostToDevice, stream), "memcpy");
-  if (snk) check(cudaMemcpyAsync(dt, snk, nodes * 4, cudaMemcpyHostToDevice, stream), "memcpy");
-  if (edge) check(cudaMemcpyAsync(de, edge, edges * 4, cudaMemcpyHostToDevice, stream), "memcpy");
+  const int32_t* ms = (const int32_t*)mapped_host_ptr(src);
+  const int32_t* mt = (const int32_t*)mapped_host_ptr(snk);
+  const int32_t* me = (const int32_t*)mapped_host_ptr(edge);
+  if ((src && !ms) || (snk && !mt) || (edge && !me)) stage.alloc(size_t(2 * nodes + edges) + 1, stream);
+  const int32_t* ds = nullptr;
+  const int32_t* dt = nullptr;
+  const int32_t* de = nullptr;
+  if (src) {
+    ds = ms;
+    if (!ds) {
+      check(cudaMemcpyAsync(stage.p, src, nodes * 4, cudaMemcpyHostToDevice, stream), "memcpy");
+      ds = stage.p;
+    }
+  }
+  if (snk) {
+    dt = mt;
+    if (!dt) {
+      check(cudaMemcpyAsync(stage.p + nodes, snk, nodes * 4, cudaMemcpyHostToDevice, stream), "memcpy");
+      dt = stage.p + nodes;
+    }
+  }
+  if (edge) {
+    de = me;
+    if (!de) {
+      check(cudaMemcpyAsync(stage.p + 2 * nodes, edge, edges * 4, cudaMemcpyHostToDevice, stream),
+            "memcpy");
+      de = stage.p + 2 * nodes;
+    }
+  }
   long long no = 0, eo = 0;
   for (size_t i = 0; i < members.size(); ++i) {
     Member& m = members[i];

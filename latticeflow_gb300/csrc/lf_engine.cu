@@ -183,7 +183,7 @@ void Engine::sync_read(void* host, const void* dev, size_t bytes) {
 // Device address of host memory the GPU reads in place (pinned, mapped into
 // the device's address space; on GB300 the reads go over NVLink-C2C), else
 // null (pageable memory is copied first).
-static const void* mapped_host_ptr(const void* p) {
+const void* mapped_host_ptr(const void* p) {
   if (!p) return nullptr;
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {

@@ -61,6 +61,9 @@ size_t pr_smem_bytes_for(const Geo& g, const Stencil& st, int elem_bytes);
 void lattice_geometry(int nd, const size_t* dims, const Stencil& st, int elem, int tile_rows,
                       Geo& g);
 Stencil make_stencil(const KernelDef* kd);
+// the device address of a pinned (page-locked) host array, which kernels can
+// read in place (over NVLink-C2C on GB300), or null for other memory
+const void* mapped_host_ptr(const void* p);
 
 class Engine : public ProfHooks {
  public:

@@ -149,3 +149,15 @@ def test_batch_packed_fill_and_results(native, gpu, oracle_port):
         off += p.n
     with pytest.raises(ValueError):
         B.addCapacitiesPacked(np.zeros(3, dtype=np.int32))
+    # pinned host arrays are read in place by the fill kernels: same results
+    import torch
+
+    def pinned(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    B.clear()
+    B.addCapacitiesPacked(pinned(np.concatenate([p.source for p in probs])),
+                          pinned(np.concatenate([p.sink for p in probs])),
+                          pinned(np.concatenate([p.edge.reshape(-1) for p in probs])))
+    B.run()
+    assert np.array_equal(B.getCutsPacked(out=pinned(np.zeros(cuts.size, np.int32))), cuts)
+    assert np.array_equal(B.flows()[1], energies)
