@@ -26,10 +26,11 @@ Stencil make_stencil(const KernelDef* kd) {
   Stencil st{};
   const int nd = kd->nd;
   st.K = kd->K;
+  // a 1-d lattice is one row of a 2-d one: its offsets run along the row
   for (int i = 0; i < st.K; ++i) {
     int a = nd == 3 ? kd->delta[i * nd + 0] : 0;
-    int b = kd->delta[i * nd + (nd == 3 ? 1 : 0)];
-    int c = kd->delta[i * nd + (nd == 3 ? 2 : 1)];
+    int b = nd == 1 ? 0 : kd->delta[i * nd + (nd == 3 ? 1 : 0)];
+    int c = kd->delta[i * nd + (nd == 3 ? 2 : nd - 1)];
     st.da[i] = (signed char)a;
     st.db[i] = (signed char)b;
     st.dc[i] = (signed char)c;
@@ -46,6 +47,19 @@ Stencil make_stencil(const KernelDef* kd) {
 // warp per row); the largest tile whose shared-memory footprint fits is used.
 void lattice_geometry(int nd, const size_t* dims, const Stencil& st, int elem, int tile_rows,
                       Geo& g) {
+  if (nd == 1) {  // one row of 1 x 32 tiles, no padding rows
+    g.A = g.B = 1;
+    g.C = int(dims[0]);
+    g.Ap = g.Bp = 1;
+    g.Cp = (g.C + 31) / 32 * 32;
+    g.NP = g.Cp;
+    g.TA = g.TB = 1;
+    g.TC = 32;
+    g.nta = g.ntb = 1;
+    g.ntc = g.Cp / 32;
+    g.ntiles = g.ntc;
+    return;
+  }
   g.A = nd == 3 ? int(dims[0]) : 1;
   g.B = int(dims[nd == 3 ? 1 : 0]);
   g.C = int(dims[nd == 3 ? 2 : 1]);
@@ -82,7 +96,7 @@ Engine::Engine(const std::string& solver, const KernelDef* k, int _nd, const siz
   dims.assign(d, d + nd);
   N = 1;
   for (size_t v : dims) N *= (long long)v;
-  if (nd != 2 && nd != 3) throw LfError{2, "only 2-d and 3-d lattices are supported"};
+  if (nd < 1 || nd > 3) throw LfError{2, "only 1-d, 2-d and 3-d lattices are supported"};
   for (size_t v : dims)
     if (v > (size_t)INT_MAX / 2) throw LfError{2, "lattice extent too large"};
   st = make_stencil(kd);

@@ -14,7 +14,9 @@
 //     divided by 2|x| (code_setup.py:163-197), each weight paired with its own
 //     offset;
 //   * names "%s%dd_%d" (code_setup.py:40); a repeated offset set becomes an
-//     alias of the first kernel that produced it (code_setup.py:369-399).
+//     alias of the first kernel that produced it (code_setup.py:369-399);
+//   * the 1-d kernels of the reference's opt-in 1-d build (Full only, integer
+//     radii 1 .. 7, code_setup.py:81-92).
 // "Full3d_26" names the 3x3x3 neighbourhood (produced by the Star rule at
 // radius 2 as "Star3d_26").
 #include <algorithm>
@@ -142,6 +144,22 @@ std::vector<KernelDef> build_registry() {
   std::vector<KernelDef> out;
   std::map<std::set<Vec>, std::string> seen_sets;
   std::set<std::string> names;
+  // The reference's opt-in 1-d build (--1d, wscript:49-67): Full kernels at
+  // the integer radii 1 .. 7 (code_setup.py:81-92), Full1d_2 .. Full1d_14.
+  for (int r = 1; r < 8; ++r) {
+    std::vector<Vec> offs = full_offsets(1, double(r));
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), "Full1d_%d", int(offs.size()));
+    KernelDef k;
+    k.name = buf;
+    k.nd = 1;
+    std::vector<double> w;
+    k.geocut = geocut_weights(1, offs, w);
+    to_lattice_order(offs, w, k);
+    seen_sets[std::set<Vec>(offs.begin(), offs.end())] = k.name;
+    names.insert(k.name);
+    out.push_back(k);
+  }
   const int max_r[4] = {0, 0, 4, 2};
   for (int dim = 2; dim <= 3; ++dim) {
     for (double r : radius_list(dim, max_r[dim])) {

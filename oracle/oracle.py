@@ -39,6 +39,12 @@ def specs():
     return _SPECS
 
 
+def registry_specs():
+    """The kernels the GPU registry serves: the reference's default build plus
+    its opt-in 1-d kernels (the opt-in 4-d kernel is not served)."""
+    return {k: v for k, v in all_specs().items() if v.dim <= 3}
+
+
 def all_specs():
     """specs() plus the kernels of the reference's opt-in 1-d and 4-d builds."""
     global _ALL_SPECS

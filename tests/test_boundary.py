@@ -32,12 +32,12 @@ def test_registry_matches_oracle(native, oracle_port):
     import latticeflow_gb300 as lf
     O = oracle_port
     names = lf.validKernelNames()
-    assert set(names) == set(O.specs())
+    assert set(names) == set(O.registry_specs())
     for k in names:
         d, w, g = lf.kernelInfo(k)
         od, ow = O.lattice_offsets(k)
-        assert np.array_equal(d, od) and np.array_equal(w, ow) and g == O.specs()[k].geocut
-        assert lf.kernelDimension(k) == O.specs()[k].dim
+        assert np.array_equal(d, od) and np.array_equal(w, ow) and g == O.registry_specs()[k].geocut
+        assert lf.kernelDimension(k) == O.registry_specs()[k].dim
 
 
 def test_registry_matches_compiled_reference_deltas(native, oracle_port):
@@ -46,9 +46,9 @@ def test_registry_matches_compiled_reference_deltas(native, oracle_port):
         pytest.skip("compiled reference not present")
     import latticeflow_gb300 as lf
     names = lf.validKernelNames()
-    assert len(names) == 20
+    assert len(names) == 27  # the 20 of the default build and the 7 of the opt-in 1-d build
     for k in names:  # every name, aliases included (the compiled reference holds them all)
-        dims = (9, 8) if lf.kernelDimension(k) == 2 else (5, 6, 7)
+        dims = {1: (12,), 2: (9, 8), 3: (5, 6, 7)}[lf.kernelDimension(k)]
         d, _, _ = lf.kernelInfo(k)
         fd = O.ref_filling_deltas(k, dims)
         assert np.array_equal(fd, d[: len(d) // 2]), k

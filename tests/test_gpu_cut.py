@@ -47,6 +47,8 @@ CASES = [
     ("Full2d_8", (70, 45)), ("Full2d_12", (40, 41)), ("Star2d_16", (37, 50)), ("Full2d_24", (30, 30)),
     ("Full2d_48", (25, 26)), ("Full3d_6", (10, 12, 40)), ("Full3d_18", (9, 9, 33)),
     ("Full3d_26", (12, 10, 35)), ("Full3d_32", (8, 9, 34)),
+    ("Full1d_2", (300,)), ("Full1d_4", (77,)), ("Full1d_6", (1,)), ("Full1d_8", (150,)),
+    ("Full1d_10", (33,)), ("Full1d_12", (64,)), ("Full1d_14", (201,)),
 ]
 
 

@@ -119,7 +119,8 @@ def test_tv_ragged_and_tiny(native, gpu, oracle_port):
 
 
 @pytest.mark.parametrize("kernel,dims", [("Full2d_4", (40, 37)), ("Full2d_8", (31, 29)),
-                                         ("Full3d_6", (9, 10, 33))])
+                                         ("Full3d_6", (9, 10, 33)), ("Full1d_4", (300,)),
+                                         ("Full1d_14", (129,))])
 def test_level_reductions_vs_oracle(native, gpu, oracle_port, kernel, dims):
     """LatticeLevelReductions through the generic interface (pf_policies.hpp:31-46)."""
     import latticeflow_gb300 as lf
