@@ -11,11 +11,11 @@
 
 namespace lfg {
 
-// kernel-size pairs compiled: every generated size alone, plus the 2-d mix of
-// 4- and 8-connected lattices
+// kernel-size pairs compiled: every generated size alone (1-d, 2-d, 3-d),
+// plus the 2-d mix of 4- and 8-connected lattices
 #define LF_POOL_PR_LIST(X) \
-  X(4, 4) X(6, 6) X(8, 8) X(12, 12) X(16, 16) X(18, 18) X(20, 20) X(24, 24) X(26, 26) \
-  X(28, 28) X(32, 32) X(36, 36) X(40, 40) X(48, 48) X(4, 8)
+  X(2, 2) X(4, 4) X(6, 6) X(8, 8) X(10, 10) X(12, 12) X(14, 14) X(16, 16) X(18, 18) \
+  X(20, 20) X(24, 24) X(26, 26) X(28, 28) X(32, 32) X(36, 36) X(40, 40) X(48, 48) X(4, 8)
 
 // Blocks that fit on the device at once for this kernel and shape (the grid
 // of a pass; its blocks stride over the queued tiles).
