@@ -9,8 +9,10 @@ push-relabel to a maximum preflow, both canonical cut sets, flow value.
   e2e    the same through the reference-facing C-ABI call with host buffers:
          addEnergyPotentials from pinned host int64 arrays (H2D inside the
          step) and the minimal cut read back into a pinned host array (D2H
-         inside the step); --e2e-handles N solves on N handles at once, one
-         host thread each, so that transfers overlap other solves
+         inside the step), on 3 handles at once by default (--e2e-handles N),
+         one host thread and stream each, so that one solve's transfer
+         overlaps another's solve, as a server runs them; e2e.one_handle is
+         the same with one handle, solve after solve
 
 The default line also carries: parity (the timed workload's energy and
 both cut sets against the oracle), batched_vs_plain (the 512-lattice batch
@@ -72,8 +74,9 @@ def parse():
                     help="one launch per pass (the default; kept for the recorded profiling commands)")
     ap.add_argument("--device-loops", action="store_true",
                     help="run the staged passes in device-side loops (CUDA graphs with conditional "
-                         "nodes, whose kernels a profiler does not list); one handle only")
-    ap.add_argument("--e2e-handles", type=int, default=1,
+                         "nodes, whose kernels a profiler does not list); one handle only: "
+                         "give --e2e-handles 1 with it")
+    ap.add_argument("--e2e-handles", type=int, default=3,
                     help="e2e with this many handles (own streams, own host threads) solving "
                          "concurrently, so one solve's host-to-device fill overlaps another's solve; "
                          "timed by the host clock around all of them")
@@ -322,7 +325,8 @@ def run_ours(args):
     elif not args.no_autotune and not args.profile_run:
         from latticeflow_gb300 import autotune
         step_device()
-        tuning, _, tune_table = autotune.tune(L, autotune.problem_key([p.kernel], p.n))
+        grid = autotune.VOLUME_GRID if len(p.dims) == 3 else None
+        tuning, _, tune_table = autotune.tune(L, autotune.problem_key([p.kernel], p.n), grid=grid)
     if args.profile_run:
         # every solve of the run (warm-up included), with the tile counters
         # that turn a capture's DRAM bytes into bytes per node visit
@@ -347,6 +351,10 @@ def run_ours(args):
     clocks = sampler.stop()
     ms_prof, _, prof, _ = timed(step_device, args.steps, True)
     e2e_timing = "CUDA events on the handle's stream"
+    for _ in range(max(1, args.warmup)):
+        step_e2e()
+    ms_e2e, _, _, _ = timed(step_e2e, args.steps, False)
+    ms_e2e_one = ms_e2e
     if args.e2e_handles > 1:
         # more handles of the same lattice, tuned alike; each thread's step is
         # the same public calls as step_e2e on its own handle and cut buffer
@@ -380,10 +388,6 @@ def run_ours(args):
         barrier()
         e2e_timing = "host clock around %d handles solving concurrently" % len(fns)
         del extra, fns
-    else:
-        for _ in range(max(1, args.warmup)):
-            step_e2e()
-        ms_e2e, _, _, _ = timed(step_e2e, args.steps, False)
 
     autotune_top = None
     if tune_table:
@@ -398,7 +402,15 @@ def run_ours(args):
     # (k_pool_pr2d for 32-bit capacities, k_pool_bfs2d for any); other
     # lattices the generic tile kernels
     tma2d = p.kernel in ("Full2d_4", "Full2d_8") and len(p.dims) == 2
-    pr_name = "k_pool_pr2d" if tma2d and elem == 4 else "k_pool_pr"
+    prk = (tuning or {}).get("pr_kernel", 0)
+    # a single 3-d lattice with a radius-1 stencil and 32-bit capacities runs
+    # the TMA-staged 3-d pass on 4-plane tiles it fits (any height for 6
+    # directions, up to 4 rows for 18 and 26)
+    rows3 = {"Full3d_6": 8, "Full3d_18": 4, "Full3d_26": 4}.get(p.kernel, 0)
+    tma3d = (len(p.dims) == 3 and elem == 4 and prk != 1 and tile[0] == 4
+             and tile[1] <= rows3)
+    pr_name = ("k_pool_pr2d" if tma2d and elem == 4 else
+               "k_pool_pr3d" if tma3d else "k_pool_pr")
     bfs_name = "k_pool_bfs2d" if tma2d else "k_pool_bfs"
     if prof["pr_ms"] >= prof["bfs_ms"]:
         kname, kbytes, kms, klaunch = pr_name, pr_bytes, prof["pr_ms"], prof["pr_launches"]
@@ -431,7 +443,8 @@ def run_ours(args):
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT,
                 "h2d_bytes_per_step": int(u.nbytes + b.nbytes),
                 "d2h_bytes_per_step": int(p.n * 4 + 24),  # the cut, flow/supply/energy
-                "handles": args.e2e_handles, "timing": e2e_timing},
+                "handles": args.e2e_handles, "timing": e2e_timing,
+                "one_handle": round(replica_value(args.steps, world, ms_e2e_one * 1e-3), 4)},
         "roofline": roofline,
         "clocks": clocks,
         "gpu_launches": int(launches),

@@ -22,6 +22,16 @@ DEFAULT_GRID = {
     "launches_per_relabel": (4, 8, 16),
 }
 
+# 3-d lattices: tiles of 4 planes x 2, 4 or 8 rows x 32 (the staged 3-d pass
+# takes 2 and 4 rows for 18 and 26 directions, every height for 6), the
+# staged pass (0) or the generic one (1)
+VOLUME_GRID = {
+    "pr_kernel": (0, 1),
+    "tile_rows": (2, 4, 8),
+    "local_sweeps": (1, 2, 4),
+    "launches_per_relabel": (4, 8, 16),
+}
+
 _memory = {}
 
 

@@ -793,10 +793,17 @@ void PoolRunner::maxflow_epochs(T* res, T* exc, int* h, uint64_t* mask, const ui
       prep_pass(cur);
       PoolPR<T> p{host[0], d_inst, d_tile_inst, res, exc, h, kmask, q, cur, R, d_counters};
       mark(0, false);
-      int k2d = 0;
+      int k2d = 0, k3d = 0;
       if constexpr (std::is_same<T, int>::value)
-        if (tune.pr_kernel != 1) k2d = pr2d_kernel_size(p, n == 1);
-      if (k2d) {
+        if (tune.pr_kernel != 1) {
+          k2d = pr2d_kernel_size(p, n == 1);
+          if (!k2d && !pmaps) k3d = pr3d_kernel_size(p, n == 1);
+        }
+      if (k3d) {
+        if constexpr (std::is_same<T, int>::value)
+          check(launch_pool_pr3d(p, k3d, d_counters + 4, std::max(tiles, 1), stream),
+                "push-relabel pass (TMA, 3-d)");
+      } else if (k2d) {
         if constexpr (std::is_same<T, int>::value)
           check(launch_pool_pr2d(p, k2d, pr2d_variant(tune.pr_kernel), d_counters + 4,
                                  std::max(tiles, 1), stream),

@@ -97,6 +97,14 @@ cudaError_t launch_pool_pr2d(const PoolPR<int>& p, int K, int variant, unsigned 
 cudaError_t launch_pool_bfs2d(const PoolBFS& p, int K, unsigned long long* fault, int tiles,
                               cudaStream_t s);
 
+// The TMA-staged 3-d push/relabel pass (lf_pool_pr3d.cu): the kernel size it
+// takes a lattice with (6, 18 or 26: a pool of one 3-d lattice, radius-1
+// neighbourhood, 4-plane tiles of 2, 4 or 8 rows whose two stage buffers fit
+// shared memory, no section mask), else 0.
+int pr3d_kernel_size(const PoolPR<int>& p, bool single);
+cudaError_t launch_pool_pr3d(const PoolPR<int>& p, int K, unsigned long long* fault, int tiles,
+                             cudaStream_t s);
+
 // Device-side loops of those passes (one CUDA graph launch runs passes until
 // the next tile list is empty or `cap` passes ran; ctl: two device words the
 // loop keeps its list index and pass count in; passes: incremented per pass;

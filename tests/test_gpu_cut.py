@@ -256,6 +256,59 @@ def test_push_relabel_kernels_agree(native, gpu, oracle_port, pr_kernel, bfs_ker
     assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
 
 
+def _random_3d(kernel, dims, seed, O):
+    rng = np.random.default_rng(seed)
+    offs, _ = O.lattice_offsets(kernel)
+    N, Kp = int(np.prod(dims)), len(offs) // 2
+    u = rng.integers(0, 120, size=(N, 2)).astype(np.int64)
+    w = rng.integers(0, 40, size=(N, Kp)).astype(np.int64)
+    b = np.zeros((N, Kp, 4), np.int64)
+    b[:, :, 1] = w
+    b[:, :, 2] = w + rng.integers(0, 3, size=(N, Kp))
+    return u, b
+
+
+@pytest.mark.parametrize("pr_kernel", [0, 1])
+@pytest.mark.parametrize("kernel,dims,tile_rows", [
+    ("Full3d_26", (12, 18, 70), 2), ("Full3d_26", (9, 20, 40), 4), ("Full3d_18", (13, 10, 45), 2),
+    ("Full3d_18", (8, 16, 33), 4), ("Full3d_6", (10, 24, 50), 8), ("Full3d_6", (7, 9, 64), 2),
+    ("Full3d_26", (5, 3, 31), 2)], ids=lambda v: str(v))
+def test_tma_pass_3d(native, gpu, oracle_port, pr_kernel, kernel, dims, tile_rows):
+    """The TMA-staged 3-d push/relabel pass (pr_kernel 0: 4 x rows x 32
+    tiles, residual planes as one 4-d box, heights with a halo as a 3-d box)
+    and the generic pass (1) give the reference's exact answer."""
+    import latticeflow_gb300 as lf
+    u, b = _random_3d(kernel, dims, 40 + tile_rows, oracle_port)
+    E, cmin, cmax, _, _ = oracle_port.port_canonical(kernel, dims, u, b)
+    L = lf.LatticeFlow(kernel, "LatticeEnergyMinimizer", dims)
+    L.setParam("pr_kernel", pr_kernel)
+    L.setTuning(tile_rows=tile_rows, local_sweeps=3, launches_per_relabel=4)
+    for _ in range(2):
+        L.clear()
+        L.addEnergyPotentials(u, b)
+        L.run()
+        assert L.layout()[0] == (4, tile_rows, 32)
+        assert L.flow()[1] == E
+        assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
+
+
+@pytest.mark.parametrize("tile_rows", [2, 4])
+def test_tma_pass_3d_volume(native, gpu, oracle_port, tile_rows):
+    """A 96^3 Full3d_26 volume (the volume workload's generator) through the
+    staged 3-d pass: the reference's energy and both cut sets."""
+    import latticeflow_gb300 as lf
+    from latticeflow_gb300 import workloads as W
+    p = W.volume_cut(2, n=96)
+    u, b = p.energies()
+    E, cmin, cmax, _, _ = oracle_port.port_canonical(p.kernel, p.dims, u, b)
+    L = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    L.setTuning(tile_rows=tile_rows, local_sweeps=2, launches_per_relabel=8)
+    L.addEnergyPotentials(u, b)
+    L.run()
+    assert L.flow()[1] == E
+    assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
+
+
 @pytest.mark.parametrize("pr_kernel", [0, 2])
 def test_tma_pass_large_cut_scaled(native, gpu, oracle_port, pr_kernel):
     import latticeflow_gb300 as lf
