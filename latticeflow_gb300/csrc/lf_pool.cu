@@ -541,6 +541,7 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
   const int chunk = tune.pass_chunk > 0 ? tune.pass_chunk : 6;
   const long long cap = 4LL * tiles + 64;
   const int k2d = tune.bfs_kernel != 1 ? lattice2d_kernel_size(host[0], n == 1) : 0;
+  const int k3d = (!k2d && tune.bfs_kernel != 1) ? lattice3d_kernel_size(host[0], n == 1) : 0;
   if (k2d && tune.device_loops == 1) {
     // the whole relabel in one device-side loop: passes until no tile is
     // queued (a cap that ends it early is reported by activate())
@@ -581,6 +582,8 @@ void PoolRunner::global_relabel(const T* res, const T* exc, int* h, uint64_t* ma
       PoolBFS p{host[0], d_inst, d_tile_inst, h, mask, q, cur, 64, d_flag, d_counters};
       mark(1, false);
       if (k2d) check(launch_pool_bfs2d(p, k2d, d_counters + 4, grid, stream), "bfs pass (TMA)");
+      else if (k3d)
+        check(launch_pool_bfs3d(p, k3d, d_counters + 4, grid, stream), "bfs pass (TMA, 3-d)");
       else if (maps)
         check(pool_bfs2d(nullptr, maps, p, tb_pool, d_counters + 4, grid, nullptr, 0, nullptr,
                          nullptr, stream),

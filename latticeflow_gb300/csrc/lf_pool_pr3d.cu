@@ -1,5 +1,6 @@
-// Launcher of the TMA-staged 3-d push/relabel pass (lf_pool_pr3d.cuh): its
-// tensor maps, launch shape, and the test of whether a pass can take it.
+// Launchers of the TMA-staged 3-d passes (push/relabel and BFS,
+// lf_pool_pr3d.cuh): their tensor maps, launch shapes, and the test of
+// whether a pass can take them.
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -29,11 +30,12 @@ PFN_cuTensorMapEncodeTiled_v12000 encode3_fn() {
 }
 
 bool encode3(CUtensorMap* m, void* base, int rank, const cuuint64_t* dims,
-             const cuuint64_t* strides, const cuuint32_t* box) {
+             const cuuint64_t* strides, const cuuint32_t* box,
+             CUtensorMapDataType type = CU_TENSOR_MAP_DATA_TYPE_INT32) {
   auto fn = encode3_fn();
   if (!fn) return false;
   const cuuint32_t es[4] = {1, 1, 1, 1};
-  return fn(m, CU_TENSOR_MAP_DATA_TYPE_INT32, rank, base, dims, strides, box, es,
+  return fn(m, type, rank, base, dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -115,15 +117,80 @@ cudaError_t launch_k3(const PR3dMaps& maps, const PoolPR<int>& p, unsigned long 
   }
 }
 
+struct Bfs3MapCache {
+  const void *h = nullptr, *mask = nullptr;
+  int Cp = 0, Bp = 0, Ap = 0, TA = 0, TB = 0;
+  BFS3dMaps maps;
+};
+
+bool bfs3_maps_for(const PoolBFS& p, int TA, int TB, BFS3dMaps& out) {
+  thread_local Bfs3MapCache c;
+  const Geo& g = p.inst0.g;
+  if (c.h == p.h && c.mask == p.mask && c.Cp == g.Cp && c.Bp == g.Bp && c.Ap == g.Ap &&
+      c.TA == TA && c.TB == TB) {
+    out = c.maps;
+    return true;
+  }
+  BFS3dMaps m;
+  const cuuint64_t d3[3] = {(cuuint64_t)g.Cp, (cuuint64_t)g.Bp, (cuuint64_t)g.Ap};
+  const cuuint64_t s4[2] = {(cuuint64_t)g.Cp * 4, (cuuint64_t)g.Cp * 4 * g.Bp};
+  const cuuint64_t s8[2] = {(cuuint64_t)g.Cp * 8, (cuuint64_t)g.Cp * 8 * g.Bp};
+  const cuuint32_t bh[3] = {(cuuint32_t)kPr3dHaloW, (cuuint32_t)(TB + 2), (cuuint32_t)(TA + 2)};
+  const cuuint32_t bm[3] = {32, (cuuint32_t)TB, (cuuint32_t)TA};
+  if (!encode3(&m.h, p.h, 3, d3, s4, bh) ||
+      !encode3(&m.mask, const_cast<uint64_t*>(p.mask), 3, d3, s8, bm,
+               CU_TENSOR_MAP_DATA_TYPE_UINT64))
+    return false;
+  c.h = p.h; c.mask = p.mask; c.Cp = g.Cp; c.Bp = g.Bp; c.Ap = g.Ap; c.TA = TA; c.TB = TB;
+  c.maps = m;
+  out = m;
+  return true;
+}
+
+template <int K, int TA, int TB>
+cudaError_t launch_b3(const BFS3dMaps& maps, const PoolBFS& p, unsigned long long* fault,
+                      int tiles, cudaStream_t s) {
+  using Ly = BFS3dLayout<TA, TB>;
+  auto kern = k_pool_bfs3d<K, TA, TB>;
+  static std::mutex mu;
+  static int cap = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!cap) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Ly::smem_bytes);
+      cap = occupancy_grid(kern, Ly::NT, Ly::smem_bytes);
+    }
+  }
+  kern<<<std::max(1, std::min(cap, tiles)), Ly::NT, Ly::smem_bytes, s>>>(maps, p, fault);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
-int pr3d_kernel_size(const PoolPR<int>& p, bool single) {
-  const InstDesc& I = p.inst0;
-  if (p.kmask || !single || !encode3_fn()) return 0;
+int lattice3d_kernel_size(const InstDesc& I, bool single) {
+  if (!single || !encode3_fn()) return 0;
   if (I.g.TC != 32 || I.g.TA != 4 || (I.g.TB != 2 && I.g.TB != 4 && I.g.TB != 8)) return 0;
   if (I.node_base != 0 || I.res_base != 0 || I.tile_base != 0 || I.plane != I.g.NP) return 0;
   if (I.g.Cp % 32 || I.g.Bp % I.g.TB || I.g.Ap % I.g.TA) return 0;
-  if (!radius1_3d(I)) return 0;
+  return radius1_3d(I) ? I.st.K : 0;
+}
+
+cudaError_t launch_pool_bfs3d(const PoolBFS& p, int K, unsigned long long* fault, int tiles,
+                              cudaStream_t s) {
+  const int TA = p.inst0.g.TA, TB = p.inst0.g.TB;
+  BFS3dMaps maps;
+  if (!bfs3_maps_for(p, TA, TB, maps)) return cudaErrorInvalidValue;
+#define LF_BFS3D(KK, BB) \
+  if (K == KK && TA == 4 && TB == BB) return launch_b3<KK, 4, BB>(maps, p, fault, tiles, s);
+  LF_BFS3D(6, 2) LF_BFS3D(6, 4) LF_BFS3D(6, 8) LF_BFS3D(18, 2) LF_BFS3D(18, 4) LF_BFS3D(18, 8)
+  LF_BFS3D(26, 2) LF_BFS3D(26, 4) LF_BFS3D(26, 8)
+#undef LF_BFS3D
+  return cudaErrorInvalidValue;
+}
+
+int pr3d_kernel_size(const PoolPR<int>& p, bool single) {
+  const InstDesc& I = p.inst0;
+  if (p.kmask || !lattice3d_kernel_size(I, single)) return 0;
   const int K = I.st.K, TB = I.g.TB;
   const bool fits = (K == 6) || (K == 18 && TB <= 4) || (K == 26 && TB <= 4);
   return fits ? K : 0;

@@ -1,6 +1,6 @@
-// Push/relabel tile pass for one 3-d lattice with a radius-1 neighbourhood
-// (Full3d_6, Full3d_18, Full3d_26) and 32-bit capacities, tiles staged into
-// shared memory by TMA.
+// Push/relabel and global-relabel BFS tile passes for one 3-d lattice with
+// a radius-1 neighbourhood (Full3d_6, Full3d_18, Full3d_26), tiles staged
+// into shared memory by TMA (push/relabel: 32-bit capacities; BFS: any).
 //
 // The algorithm and the hazards are those of the 2-d staged pass
 // (lf_pool_pr2d.cuh): up to `sweeps` rounds of a push phase with frozen
@@ -24,6 +24,7 @@
 #include <cuda.h>
 
 #include "lf_pool.cuh"
+#include "lf_pool_graph.cuh"
 #include "lf_pool_pr2d.cuh"
 #include "lf_tile_common.cuh"
 
@@ -298,6 +299,194 @@ __global__ void __launch_bounds__(TA * TB * 32, PR3dLayout<K, TA, TB>::min_block
                          reinterpret_cast<int*>(stg + Ly::res_bytes),
                          reinterpret_cast<int*>(stg + Ly::res_bytes + Ly::exc_bytes), gt, e0, h0,
                          s_nbr + buf);
+  }
+}
+
+// ------------------------------------------------------------ 3-d BFS
+//
+// The relaxation of the 2-d staged BFS (lf_pool_bfs2d.cuh) on 4 x TB x 32
+// tiles: exact distance to the nearest deficit along residual edges,
+// iterated inside the tile until stable, rows (the c axis, directions 0 and
+// K/2 of every 3-d stencil) relaxed whole by segmented warp min-scans.  One
+// elected thread stages a visit with two bulk tensor copies: the heights
+// with their halo (3-d box {40 x (TB + 2) x 6} from (c0 - 4, b0 - 1, a0 - 1))
+// and the 64-bit masks (3-d box {32 x TB x 4}).  A changed node queues the
+// tiles that hold its neighbours across the tile edge.
+
+struct BFS3dMaps {
+  CUtensorMap h;     // 3-d {Cp, Bp, Ap}, 32-bit
+  CUtensorMap mask;  // 3-d {Cp, Bp, Ap}, 64-bit
+};
+
+template <int TA, int TB>
+struct BFS3dLayout {
+  static constexpr int NT = TA * TB * 32;
+  static constexpr int HB = TB + 2;
+  static constexpr int h_bytes = (TA + 2) * HB * kPr3dHaloW * 4;
+  static constexpr int mask_off = (h_bytes + 127) / 128 * 128;
+  static constexpr int mask_bytes = NT * 8;
+  static constexpr int stage_bytes = (mask_off + mask_bytes + 127) / 128 * 128;
+  static constexpr int tx_bytes = h_bytes + mask_bytes;
+  // two stage buffers, two mbarriers, an edge-flag word per buffer, alignment slack
+  static constexpr int smem_bytes = 2 * stage_bytes + 32 + 128;
+};
+
+template <int TA, int TB>
+__device__ __forceinline__ void bfs3d_issue(const BFS3dMaps& maps, const Geo& g, int tile,
+                                            unsigned stage, unsigned bar) {
+  using Ly = BFS3dLayout<TA, TB>;
+  if (!tile_ok(tile, g.ntiles)) {
+    mbar_expect_tx(bar, 0);
+    return;
+  }
+  const int tc = tile % g.ntc, tb = (tile / g.ntc) % g.ntb, ta = tile / (g.ntc * g.ntb);
+  const int a0 = ta * TA, b0 = tb * TB, c0 = tc * 32;
+  mbar_expect_tx(bar, Ly::tx_bytes);
+  tma_load_3d(stage, &maps.h, c0 - 4, b0 - 1, a0 - 1, bar);
+  tma_load_3d(stage + Ly::mask_off, &maps.mask, c0, b0, a0, bar);
+}
+
+template <int K, int TA, int TB>
+__device__ __forceinline__ void bfs3d_tile(const PoolBFS& p, const Geo& g, int cur,
+                                           unsigned char* stage, unsigned* s_flags, int tile,
+                                           int my_h, const uint64_t m) {
+  constexpr int HW = kPr3dHaloW;
+  constexpr int HB = TB + 2;
+  int* s_h = reinterpret_cast<int*>(stage);
+  const int t = threadIdx.x;
+  const int ic = t & 31, ib = (t >> 5) % TB, ia = t / (32 * TB);
+  const int tc = tile % g.ntc, tb = (tile / g.ntc) % g.ntb, ta = tile / (g.ntc * g.ntb);
+  const long long gi = ((long long)(ta * TA + ia) * g.Bp + (tb * TB + ib)) * g.Cp + (tc * 32 + ic);
+  const int hidx = ((ia + 1) * HB + (ib + 1)) * HW + (ic + 4);
+  const int nxt = cur ^ 1;
+  // the row directions of every 3-d stencil: (0, 0, 1) is entry 0,
+  // (0, 0, -1) entry K/2
+  constexpr int kr = 0, kl = K / 2;
+  const bool can_l = (m >> kl) & 1, can_r = (m >> kr) & 1;
+  bool changed = false;
+  int converged = 0;
+  for (int it = 0; it < p.max_local; ++it) {
+    int best = my_h;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if ((m >> k) & 1) {
+        const int hn = s_h[hidx + (s3_da<K>(k) * HB + s3_db<K>(k)) * HW + s3_dc<K>(k)] + 1;
+        best = hn < best ? hn : best;
+      }
+    }
+    // after the first iteration the row is consistent along its row edges,
+    // and stays so while no node of the row improves
+    if (it == 0 || __any_sync(0xffffffffu, best < my_h)) {
+      best = row_scan_from_left(best, can_l, ic);
+      best = row_scan_from_right(best, can_r, ic);
+    }
+    const int c = best < my_h;
+    if (c) {
+      my_h = best;
+      s_h[hidx] = best;
+      changed = true;
+    }
+    if (!__syncthreads_or(c)) {
+      converged = 1;
+      break;
+    }
+  }
+  if (changed) p.h[gi] = my_h;
+  // tiles that hold the neighbours of changed nodes across the tile edge
+  unsigned bits = 0;
+  if (changed) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int da = s3_da<K>(k), db = s3_db<K>(k), dc = s3_dc<K>(k);
+      const int dta = (da < 0 && ia == 0) ? -1 : (da > 0 && ia == TA - 1) ? 1 : 0;
+      const int dtb = (db < 0 && ib == 0) ? -1 : (db > 0 && ib == TB - 1) ? 1 : 0;
+      const int dtc = (dc < 0 && ic == 0) ? -1 : (dc > 0 && ic == 31) ? 1 : 0;
+      if (dta || dtb || dtc) bits |= nbr_bit3(dta, dtb, dtc);
+    }
+  }
+  bits = __reduce_or_sync(0xffffffffu, bits);
+  if (ic == 0 && bits) atomicOr(s_flags, bits);
+  // the buffer's next contents come from the async proxy
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  const unsigned f = *s_flags;
+  if (t < 27 && t != 13 && ((f >> t) & 1u)) {
+    const int a = ta + t / 9 - 1, b = tb + (t / 3) % 3 - 1, c = tc + t % 3 - 1;
+    if (a >= 0 && a < g.nta && b >= 0 && b < g.ntb && c >= 0 && c < g.ntc)
+      enqueue_tile(p.q, nxt, (a * g.ntb + b) * g.ntc + c);
+  }
+  if (t == 0) {
+    if (f) *p.any_changed = 1;
+    if (!converged) {
+      enqueue_tile(p.q, nxt, tile);
+      *p.any_changed = 1;
+    }
+  }
+}
+
+// One 3-d lattice (the pool of one), one launch per pass.  `fault` as for
+// k_pool_pr3d.
+template <int K, int TA, int TB>
+__global__ void __launch_bounds__(TA * TB * 32, 1536 / (TA * TB * 32))
+    k_pool_bfs3d(const __grid_constant__ BFS3dMaps maps, const __grid_constant__ PoolBFS p,
+                 unsigned long long* fault) {
+  using Ly = BFS3dLayout<TA, TB>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<unsigned long long>(smem_raw) + 127) & ~127ull);
+  const unsigned bar0 = smem_addr(smem + 2 * Ly::stage_bytes);  // two mbarriers, 8 bytes apart
+  // edge flags of the visit on each buffer: a word is cleared two visits
+  // after its last readers, who have passed two barriers since
+  unsigned* s_flags = reinterpret_cast<unsigned*>(smem + 2 * Ly::stage_bytes + 16);
+  const unsigned stage0 = smem_addr(smem);
+  const Geo& g = p.inst0.g;
+  const int cur = p.cur;
+  const unsigned n = queued_count(p.q, cur);
+  const int* list = p.q.list[cur];
+  if (blockIdx.x >= n) return;
+  if (threadIdx.x == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar0 + 8, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const bool done = p.inst0.done != 0;
+  if (threadIdx.x == 0 && !done) bfs3d_issue<TA, TB>(maps, g, list[blockIdx.x], stage0, bar0);
+  unsigned phases = 0;
+  unsigned buf = 0;
+  for (unsigned i = blockIdx.x; i < n; i += gridDim.x, buf ^= 1) {
+    const int gt = list[i];
+    if (threadIdx.x == 0) {
+      p.q.flag[cur][gt] = 0;
+      atomicAdd(&p.counters[1], 1ull);
+      s_flags[buf] = 0;
+    }
+    if (done) continue;
+    const unsigned nx = i + gridDim.x;
+    if (threadIdx.x == 0 && nx < n)
+      bfs3d_issue<TA, TB>(maps, g, list[nx], stage0 + (buf ^ 1) * Ly::stage_bytes,
+                          bar0 + (buf ^ 1) * 8);
+    const unsigned bar = bar0 + buf * 8;
+    const unsigned par = (phases >> buf) & 1u;
+    const bool ok = mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+    phases ^= 1u << buf;
+    unsigned char* stg = smem + buf * Ly::stage_bytes;
+    const int ia = threadIdx.x / (32 * TB), ib = (threadIdx.x >> 5) % TB, ic = threadIdx.x & 31;
+    const int h0 = reinterpret_cast<const int*>(stg)[((ia + 1) * Ly::HB + (ib + 1)) * kPr3dHaloW +
+                                                      ic + 4];
+    const uint64_t m = reinterpret_cast<const uint64_t*>(stg + Ly::mask_off)[threadIdx.x];
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicExch(fault, 1ull);
+      mbar_wait_bounded(bar, par, kPr2dWaitLimit);
+      if (nx < n) mbar_wait_bounded(bar0 + (buf ^ 1) * 8, (phases >> (buf ^ 1)) & 1u, kPr2dWaitLimit);
+      return;
+    }
+    if (!tile_ok(gt, g.ntiles)) {
+      if (threadIdx.x == 0) atomicExch(fault, 2ull);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      continue;
+    }
+    bfs3d_tile<K, TA, TB>(p, g, cur, stg, s_flags + buf, gt, h0, m);
   }
 }
 

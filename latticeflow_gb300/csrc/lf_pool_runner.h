@@ -104,6 +104,12 @@ cudaError_t launch_pool_bfs2d(const PoolBFS& p, int K, unsigned long long* fault
 int pr3d_kernel_size(const PoolPR<int>& p, bool single);
 cudaError_t launch_pool_pr3d(const PoolPR<int>& p, int K, unsigned long long* fault, int tiles,
                              cudaStream_t s);
+// The TMA-staged 3-d BFS pass: the kernel size it takes a lattice with (a
+// pool of one 3-d lattice, radius-1 neighbourhood, 4-plane tiles of 2, 4 or
+// 8 rows; any capacity type), else 0.
+int lattice3d_kernel_size(const InstDesc& I, bool single);
+cudaError_t launch_pool_bfs3d(const PoolBFS& p, int K, unsigned long long* fault, int tiles,
+                              cudaStream_t s);
 
 // Device-side loops of those passes (one CUDA graph launch runs passes until
 // the next tile list is empty or `cap` passes ran; ctl: two device words the

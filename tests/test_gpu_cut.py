@@ -268,20 +268,22 @@ def _random_3d(kernel, dims, seed, O):
     return u, b
 
 
-@pytest.mark.parametrize("pr_kernel", [0, 1])
+@pytest.mark.parametrize("pr_kernel,bfs_kernel", [(0, 0), (1, 1), (0, 1), (1, 0)])
 @pytest.mark.parametrize("kernel,dims,tile_rows", [
     ("Full3d_26", (12, 18, 70), 2), ("Full3d_26", (9, 20, 40), 4), ("Full3d_18", (13, 10, 45), 2),
     ("Full3d_18", (8, 16, 33), 4), ("Full3d_6", (10, 24, 50), 8), ("Full3d_6", (7, 9, 64), 2),
     ("Full3d_26", (5, 3, 31), 2)], ids=lambda v: str(v))
-def test_tma_pass_3d(native, gpu, oracle_port, pr_kernel, kernel, dims, tile_rows):
-    """The TMA-staged 3-d push/relabel pass (pr_kernel 0: 4 x rows x 32
-    tiles, residual planes as one 4-d box, heights with a halo as a 3-d box)
-    and the generic pass (1) give the reference's exact answer."""
+def test_tma_pass_3d(native, gpu, oracle_port, pr_kernel, bfs_kernel, kernel, dims, tile_rows):
+    """The TMA-staged 3-d passes (pr_kernel / bfs_kernel 0: 4 x rows x 32
+    tiles; push/relabel with the residual planes as one 4-d box, BFS with
+    heights and masks as 3-d boxes) and the generic passes (1), in every
+    combination, give the reference's exact answer."""
     import latticeflow_gb300 as lf
     u, b = _random_3d(kernel, dims, 40 + tile_rows, oracle_port)
     E, cmin, cmax, _, _ = oracle_port.port_canonical(kernel, dims, u, b)
     L = lf.LatticeFlow(kernel, "LatticeEnergyMinimizer", dims)
     L.setParam("pr_kernel", pr_kernel)
+    L.setParam("bfs_kernel", bfs_kernel)
     L.setTuning(tile_rows=tile_rows, local_sweeps=3, launches_per_relabel=4)
     for _ in range(2):
         L.clear()
