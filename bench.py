@@ -11,8 +11,10 @@ push-relabel to a maximum preflow, both canonical cut sets, flow value.
          step) and the minimal cut read back into a pinned host array (D2H
          inside the step), on 3 handles at once by default (--e2e-handles N),
          one host thread and stream each, so that one solve's transfer
-         overlaps another's solve, as a server runs them; e2e.one_handle is
-         the same with one handle, solve after solve
+         overlaps another's solve, as a server runs them; each handle's
+         energies go through the copy engine into a device buffer it keeps
+         (--host-stage 1); e2e.one_handle is one handle, solve after solve,
+         with the fill kernel reading the pinned arrays in place
 
 The default line also carries: parity (the timed workload's energy and
 both cut sets against the oracle), batched_vs_plain (the 512-lattice batch
@@ -80,6 +82,12 @@ def parse():
                     help="e2e with this many handles (own streams, own host threads) solving "
                          "concurrently, so one solve's host-to-device fill overlaps another's solve; "
                          "timed by the host clock around all of them")
+    ap.add_argument("--host-stage", type=int, default=1, choices=[0, 1],
+                    help="e2e on several handles: pinned host energies copied into HBM by "
+                         "the copy engine first (1, so that the SMs stay free for the other "
+                         "handles' solves during a transfer) or read in place by the fill "
+                         "kernel (0); e2e.one_handle always reads in place, the faster form "
+                         "for solves run one after another")
     ap.add_argument("--tuning", default=None,
                     help="tile_rows,local_sweeps,launches_per_relabel instead of the autotuner "
                          "(e.g. the setting a bench run chose, for a profile run)")
@@ -351,11 +359,13 @@ def run_ours(args):
     clocks = sampler.stop()
     ms_prof, _, prof, _ = timed(step_device, args.steps, True)
     e2e_timing = "CUDA events on the handle's stream"
+    L.setParam("host_stage", 0 if args.e2e_handles > 1 else args.host_stage)
     for _ in range(max(1, args.warmup)):
         step_e2e()
     ms_e2e, _, _, _ = timed(step_e2e, args.steps, False)
     ms_e2e_one = ms_e2e
     if args.e2e_handles > 1:
+        L.setParam("host_stage", args.host_stage)
         # more handles of the same lattice, tuned alike; each thread's step is
         # the same public calls as step_e2e on its own handle and cut buffer
         extra = []
@@ -363,6 +373,7 @@ def run_ours(args):
             Lx = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
             for k_, v_ in (tuning or {}).items():
                 Lx.setParam(k_, v_)
+            Lx.setParam("host_stage", args.host_stage)
             cx = torch.empty(p.n, dtype=torch.int32).pin_memory()
             extra.append((Lx, cx))
 
@@ -444,6 +455,9 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(u.nbytes + b.nbytes),
                 "d2h_bytes_per_step": int(p.n * 4 + 24),  # the cut, flow/supply/energy
                 "handles": args.e2e_handles, "timing": e2e_timing,
+                "host_read": ("copy engine into HBM, then fill" if args.host_stage else
+                              "fill kernel reads the pinned arrays in place")
+                             + ("; one_handle: in place" if args.e2e_handles > 1 else ""),
                 "one_handle": round(replica_value(args.steps, world, ms_e2e_one * 1e-3), 4)},
         "roofline": roofline,
         "clocks": clocks,

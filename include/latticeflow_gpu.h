@@ -160,15 +160,18 @@ int lf_set_tuning(lf_lattice* h, int tile_rows, int local_sweeps, int launches_p
  * solve gives up with LF_ERR_NO_CONVERGENCE; 0 = 1,000,000; the handle stays
  * usable), "pr_kernel" (push/relabel pass of 2-d 3x3 lattices: 0 = staged by
  * bulk tensor copies, 40 registers; 1 = generic tile kernel; 2 = staged, 32
- * registers; 3 = staged, one warp per tile, launched one pass at a time),
+ * registers; 3 = staged, one warp per tile, launched one pass at a time; 3-d
+ * lattices with a radius-1 neighbourhood: 0, 2 and 3 = staged, 1 = generic),
  * "bfs_kernel" (global-relabel pass of those lattices: 0 =
  * staged, 1 = generic), "device_loops" (1 = the staged passes of a relabel or
  * an epoch run as one CUDA graph with a device-side loop; 0 = one launch per
  * pass, the default), "fill_kernel" (energy fill of device-resident arrays:
  * 0 = gathered with one lane per filling edge, 1 = gathered per node, 2 =
  * scattered with atomics, the form always used for pinned host arrays read
- * in place).  Results never depend on these.  LF_ERR_INVALID for an
- * unknown name. */
+ * in place), "host_stage" (pinned host energies: 0 = read in place by the
+ * fill kernel, the default; 1 = copied into device memory by the copy
+ * engine first, then filled from there).  Results never depend on these.
+ * LF_ERR_INVALID for an unknown name. */
 int lf_set_param(lf_lattice* h, const char* name, int value);
 
 /* -------------------------------------------------------------- batches

@@ -256,6 +256,7 @@ int lf_set_param(lf_lattice* h, const char* name, int value) {
     else if (n == "bfs_kernel") t.bfs_kernel = value;
     else if (n == "device_loops") t.device_loops = value;
     else if (n == "fill_kernel") t.fill_kernel = value;
+    else if (n == "host_stage") t.host_stage = value;
     else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
   });
 }

@@ -132,6 +132,7 @@ Engine::~Engine() {
   cudaFree(d_sum);
   cudaFree(d_kmask);
   cudaFree(d_cuts);
+  cudaFree(d_stage);
   if (h_pinned) cudaFreeHost(h_pinned);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
@@ -216,10 +217,30 @@ void Engine::add_energy(const int64_t* unary, const int64_t* binary, bool device
   // transfer overlaps the fill instead of preceding it
   const int64_t* mu = device_ptrs ? nullptr : (const int64_t*)mapped_host_ptr(unary);
   const int64_t* mb = device_ptrs ? nullptr : (const int64_t*)mapped_host_ptr(binary);
-  const bool in_place = mu && mb;  // read over the host link: each table once (scatter)
+  // read over the host link: each table once (scatter); or staged by the
+  // copy engine like pageable arrays, then filled from HBM
+  const bool in_place = mu && mb && tune.host_stage != 1;
   if (in_place) {
     du = mu;
     db = mb;
+    device_ptrs = true;
+  } else if (mu && mb) {
+    // host_stage: the copy engine moves the pinned tables into a device
+    // buffer the engine keeps (no allocation per call), the fill reads HBM
+    if (stage_bytes < ub + bb) {
+      check(cudaStreamSynchronize(stream), "sync");
+      cudaFree(d_stage);
+      d_stage = nullptr;
+      stage_bytes = 0;
+      check(cudaMalloc(&d_stage, ub + bb), "cudaMalloc staging");
+      stage_bytes = ub + bb;
+    }
+    int64_t* su = static_cast<int64_t*>(d_stage);
+    int64_t* sb = su + ub / sizeof(int64_t);
+    check(cudaMemcpyAsync(su, unary, ub, cudaMemcpyHostToDevice, stream), "memcpy unary");
+    check(cudaMemcpyAsync(sb, binary, bb, cudaMemcpyHostToDevice, stream), "memcpy binary");
+    du = su;
+    db = sb;
     device_ptrs = true;
   }
   if (!device_ptrs) {

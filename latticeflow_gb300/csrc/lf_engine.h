@@ -102,6 +102,8 @@ class Engine : public ProfHooks {
   uint64_t* d_mask = nullptr;
   uint64_t* d_kmask = nullptr;
   int* d_mark = nullptr;
+  void* d_stage = nullptr;  // host_stage: device copy of pinned energies (kept)
+  size_t stage_bytes = 0;
   unsigned long long* d_u64 = nullptr;  // [1] range bound
   long long* d_sum = nullptr;           // [0] stuck excess, [1] initial supply
   int* h_pinned = nullptr;              // small pinned scratch

@@ -37,6 +37,10 @@ struct Tuning {
                                  // lane per filling edge where K / 2 divides a warp (else
                                  // per node), 1 = gathered per node, 2 = scattered with
                                  // atomics (pinned host arrays read in place: always 2)
+  int host_stage = 0;            // pinned host energies: 0 = read in place by the fill
+                                 // kernel over the host link, 1 = copied into HBM by the
+                                 // copy engine first (the SMs stay free for other solves
+                                 // during the transfer)
 };
 
 struct SolveStats {

@@ -212,6 +212,16 @@ def test_pinned_host_arrays_read_in_place(native, gpu):
     c.run()
     assert a.flow() == c.flow()
     assert np.array_equal(a.getCut(), c.getCut()) and np.array_equal(a.getCutMax(), c.getCutMax())
+    # the same pinned arrays staged into device memory by the copy engine
+    s = lf.LatticeFlow(p.kernel, "LatticeEnergyMinimizer", p.dims)
+    s.setParam("host_stage", 1)
+    for _ in range(2):
+        s.clear()
+        N.check(N.lib().lf_add_energy_potentials(s._h, ctypes.c_void_p(pu.data_ptr()),
+                                                 ctypes.c_void_p(pb.data_ptr())))
+        s.run()
+        assert s.flow() == c.flow()
+        assert np.array_equal(s.getCut(), c.getCut()) and np.array_equal(s.getCutMax(), c.getCutMax())
     # capacities
     ps = torch.from_numpy(p.source).pin_memory()
     pk = torch.from_numpy(p.sink).pin_memory()
