@@ -54,6 +54,14 @@ def test_volume_cut_256_vs_oracle(native, gpu, oracle_port):
     L.addCapacities(p.source, p.sink, p.edge)
     L.run()
     _check_cut(L, E, cmin, cmax)
+    # the staged 3-d passes at the bench's setting (2-row tiles: staged
+    # push/relabel and BFS), the same answer at full size
+    L.setTuning(tile_rows=2, local_sweeps=2, launches_per_relabel=16)
+    L.clear()
+    L.addCapacities(p.source, p.sink, p.edge)
+    L.run()
+    assert L.layout()[0] == (4, 2, 32)
+    _check_cut(L, E, cmin, cmax)
 
 
 def test_batch_512_vs_oracle(native, gpu, oracle_port):
