@@ -676,12 +676,12 @@ PathGPU::PathGPU(Engine& e, const std::vector<int64_t>& base_rowmajor,
   // lattice: a short pass cadence between relabels (the parametric flow's
   // 64 passes are for sections that span the lattice)
   E.tune.launches_per_relabel = 8;
-  // region probes too large for one block run on the generic tile passes,
-  // without the tail step: a region probe is a max-flow confined to a
-  // small part of the lattice by its section mask, which those passes
-  // handle with no staging geometry
-  E.tune.pr_kernel = 1;
-  E.tune.bfs_kernel = 1;
+  // region probes too large for one block run on the staged 64-bit passes
+  // with the section mask (pr_kernel / bfs_kernel 0; measured at 256^2:
+  // 17.1 s of large probes against 19.5 s on the generic tile passes),
+  // without the tail step
+  E.tune.pr_kernel = 0;
+  E.tune.bfs_kernel = 0;
   E.tune.tail_active = -1;
   ck(cudaStreamSynchronize(s), "sync");
 }
