@@ -13,6 +13,7 @@
 #include "lf_pool_pr2d.cuh"
 #include "lf_pool_launch.cuh"
 #include "lf_pool_runner.h"
+#include "lf_tensor_map.h"
 
 namespace lfg {
 
@@ -26,29 +27,12 @@ bool stencil_is(const Stencil& st) {
   return true;
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  });
-  return fn;
-}
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() { return tensor_map_encoder(); }
 
 bool encode(CUtensorMap* m, void* base, int rank, const cuuint64_t* dims,
             const cuuint64_t* strides, const cuuint32_t* box,
             CUtensorMapDataType type = CU_TENSOR_MAP_DATA_TYPE_INT32) {
-  auto fn = encode_fn();
-  if (!fn) return false;
-  const cuuint32_t es[3] = {1, 1, 1};
-  return fn(m, type, rank, base, dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  return encode_tensor_map(m, base, rank, dims, strides, box, type);
 }
 
 // Tensor maps of the last lattice this host thread launched for (a solve

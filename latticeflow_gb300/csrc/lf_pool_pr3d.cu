@@ -1,44 +1,17 @@
 // Launchers of the TMA-staged 3-d passes (push/relabel and BFS,
 // lf_pool_pr3d.cuh): their tensor maps, launch shapes, and the test of
 // whether a pass can take them.
-#include <cudaTypedefs.h>
-
 #include <algorithm>
-#include <cstdlib>
 #include <mutex>
 
 #include "lf_pool_launch.cuh"
 #include "lf_pool_pr3d.cuh"
 #include "lf_pool_runner.h"
+#include "lf_tensor_map.h"
 
 namespace lfg {
 
 namespace {
-
-PFN_cuTensorMapEncodeTiled_v12000 encode3_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  });
-  return fn;
-}
-
-bool encode3(CUtensorMap* m, void* base, int rank, const cuuint64_t* dims,
-             const cuuint64_t* strides, const cuuint32_t* box,
-             CUtensorMapDataType type = CU_TENSOR_MAP_DATA_TYPE_INT32) {
-  auto fn = encode3_fn();
-  if (!fn) return false;
-  const cuuint32_t es[4] = {1, 1, 1, 1};
-  return fn(m, type, rank, base, dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
 
 // the lattice's stencil is the compile-time table of that size
 template <int K>
@@ -84,8 +57,9 @@ bool maps3_for(const PoolPR<int>& p, int K, int TA, int TB, PR3dMaps& out) {
   const cuuint64_t s3[2] = {row, pl};
   const cuuint32_t be[3] = {32, (cuuint32_t)TB, (cuuint32_t)TA};
   const cuuint32_t bh[3] = {(cuuint32_t)kPr3dHaloW, (cuuint32_t)(TB + 2), (cuuint32_t)(TA + 2)};
-  if (!encode3(&m.res, p.res, 4, d4, s4, b4) || !encode3(&m.exc, p.exc, 3, d3, s3, be) ||
-      !encode3(&m.h, p.h, 3, d3, s3, bh))
+  if (!encode_tensor_map(&m.res, p.res, 4, d4, s4, b4) ||
+      !encode_tensor_map(&m.exc, p.exc, 3, d3, s3, be) ||
+      !encode_tensor_map(&m.h, p.h, 3, d3, s3, bh))
     return false;
   c.res = p.res; c.exc = p.exc; c.h = p.h;
   c.Cp = g.Cp; c.Bp = g.Bp; c.Ap = g.Ap; c.K = K; c.TA = TA; c.TB = TB;
@@ -137,8 +111,8 @@ bool bfs3_maps_for(const PoolBFS& p, int TA, int TB, BFS3dMaps& out) {
   const cuuint64_t s8[2] = {(cuuint64_t)g.Cp * 8, (cuuint64_t)g.Cp * 8 * g.Bp};
   const cuuint32_t bh[3] = {(cuuint32_t)kPr3dHaloW, (cuuint32_t)(TB + 2), (cuuint32_t)(TA + 2)};
   const cuuint32_t bm[3] = {32, (cuuint32_t)TB, (cuuint32_t)TA};
-  if (!encode3(&m.h, p.h, 3, d3, s4, bh) ||
-      !encode3(&m.mask, const_cast<uint64_t*>(p.mask), 3, d3, s8, bm,
+  if (!encode_tensor_map(&m.h, p.h, 3, d3, s4, bh) ||
+      !encode_tensor_map(&m.mask, const_cast<uint64_t*>(p.mask), 3, d3, s8, bm,
                CU_TENSOR_MAP_DATA_TYPE_UINT64))
     return false;
   c.h = p.h; c.mask = p.mask; c.Cp = g.Cp; c.Bp = g.Bp; c.Ap = g.Ap; c.TA = TA; c.TB = TB;
@@ -168,7 +142,7 @@ cudaError_t launch_b3(const BFS3dMaps& maps, const PoolBFS& p, unsigned long lon
 }  // namespace
 
 int lattice3d_kernel_size(const InstDesc& I, bool single) {
-  if (!single || !encode3_fn()) return 0;
+  if (!single || !tensor_map_encoder()) return 0;
   if (I.g.TC != 32 || I.g.TA != 4 || (I.g.TB != 2 && I.g.TB != 4 && I.g.TB != 8)) return 0;
   if (I.node_base != 0 || I.res_base != 0 || I.tile_base != 0 || I.plane != I.g.NP) return 0;
   if (I.g.Cp % 32 || I.g.Bp % I.g.TB || I.g.Ap % I.g.TA) return 0;
