@@ -578,13 +578,22 @@ def run_batch(args):
     snk_all = pinned(np.concatenate([p.sink for p in probs]))
     edge_all = pinned(np.concatenate([p.edge.reshape(-1) for p in probs]))
     cut_buf = pinned(np.zeros(int(sum(p.n for p in probs)), dtype=np.int32))
-    cut_bytes = 0
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+    # one batch at a time: the fill kernel reading the pinned arrays in place
+    # overlaps the transfer with the fill (8.9k against 8.1k solves/s with the
+    # copy-engine staging, untuned)
+    B.setParam("host_stage", 0)
+
+    def step_e2e():
         B.clear()
         B.addCapacitiesPacked(src_all, snk_all, edge_all)
         B.run()
         B.getCutsPacked(out=cut_buf)
+
+    step_e2e()  # the staging buffer is allocated once
+    cut_bytes = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
         cut_bytes += cut_buf.nbytes
     wall_e2e = time.perf_counter() - t0
     n = len(probs)
@@ -602,7 +611,8 @@ def run_batch(args):
                    "tuning": setting, "autotuned": setting is not None,
                    "l2": "inputs larger than L2 (no flush needed)"},
         "e2e": {"value": round(replica_value(n * args.steps, world, wall_e2e), 3), "unit": UNIT,
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(cut_bytes / args.steps)},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(cut_bytes / args.steps),
+                "host_read": "the fill kernel reads the pinned arrays in place"},
         "wall_ms_per_step": round(1e3 * wall / args.steps, 3),
         "clocks": clocks,
         "batched_vs_plain": summary,

@@ -9,8 +9,179 @@
 #include <cstring>
 
 #include "lf_batch.h"
+#include "lf_tile_common.cuh"
 
 namespace lfg {
+
+// ------------------------------------------------ batch-wide element kernels
+//
+// One launch over the elements of every lattice of the batch instead of one
+// launch per lattice: a thread finds its lattice by binary search over the
+// lattices' first elements (a table in device memory, rebuilt when the
+// layout changes), then does what the per-lattice kernel does for that
+// element.
+
+struct BatchMember {
+  Geo g;
+  Stencil st;
+  long long node_base, res_base;  // the lattice's first node / residual word in the pools
+  long long node_off, edge_off;   // its first node / filling edge in packed host arrays
+  int nd;
+};
+
+// largest i in [0, nm) with begin[i] <= x (begin ascending, begin[0] = 0)
+__device__ __forceinline__ int batch_member_of(const long long* begin, int nm, long long x) {
+  int lo = 0, hi = nm - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (begin[mid] <= x) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ long long batch_local_node(const BatchMember& m, long long b) {
+  int a, bb, c;
+  if (m.nd == 2) { a = 0; bb = int(b / m.g.C); c = int(b % m.g.C); }
+  else { c = int(b % m.g.C); bb = int((b / m.g.C) % m.g.B); a = int(b / ((long long)m.g.C * m.g.B)); }
+  return ((long long)a * m.g.Bp + bb) * m.g.Cp + c;
+}
+
+// k_fill_caps (capacity form, plain scale) for every lattice: thread = one
+// (node, filling edge) of the packed arrays; the constant term is summed per
+// warp when the whole warp serves one lattice, else per thread.
+__global__ void k_fill_caps_batch(const BatchMember* M, const long long* edge_begin, int nm,
+                                  long long total, const int32_t* src, const int32_t* snk,
+                                  const int32_t* edge, long long* exc, long long* cap,
+                                  long long* c0sum, int* err) {
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int i = -1;
+  long long c0 = 0;
+  if (tid < total) {
+    i = batch_member_of(edge_begin, nm, tid);
+    const BatchMember& m = M[i];
+    const int Kp = m.st.K / 2;
+    const long long local = tid - edge_begin[i];
+    const long long b = local / Kp;
+    const int e = int(local % Kp);
+    int a, bb, c;
+    if (m.nd == 2) { a = 0; bb = int(b / m.g.C); c = int(b % m.g.C); }
+    else { c = int(b % m.g.C); bb = int((b / m.g.C) % m.g.B); a = int(b / ((long long)m.g.C * m.g.B)); }
+    const long long u = ((long long)a * m.g.Bp + bb) * m.g.Cp + c;
+    if (e == 0) {
+      const long long sv = src ? src[m.node_off + b] : 0, tv = snk ? snk[m.node_off + b] : 0;
+      if (sv < 0 || tv < 0) atomicExch(err, 1);
+      if (sv - tv) atom_add(&exc[m.node_base + u], sv - tv);
+      c0 += sv;
+    }
+    if (edge) {
+      const long long w = edge[m.edge_off + b * Kp + e];
+      const int na = a + m.st.da[e], nb = bb + m.st.db[e], nc = c + m.st.dc[e];
+      if (w < 0) atomicExch(err, 1);
+      if (w > 0 && na >= 0 && na < m.g.A && nb >= 0 && nb < m.g.B && nc >= 0 && nc < m.g.C) {
+        const long long v = ((long long)na * m.g.Bp + nb) * m.g.Cp + nc;
+        atom_add(&cap[m.res_base + (long long)e * m.g.NP + u], w);
+        atom_add(&cap[m.res_base + (long long)m.st.rev[e] * m.g.NP + v], w);
+      }
+    }
+  }
+  const int i0 = __shfl_sync(0xffffffffu, i, 0);
+  if (__all_sync(0xffffffffu, i == i0)) {
+    for (int o = 16; o > 0; o >>= 1) c0 += __shfl_down_sync(0xffffffffu, c0, o);
+    if ((threadIdx.x & 31) == 0 && i0 >= 0 && c0) atom_add(&c0sum[i0], c0);
+  } else if (i >= 0 && c0) {
+    atom_add(&c0sum[i], c0);
+  }
+}
+
+// k_range_bound for every lattice: thread = one padded node of the pools
+__global__ void k_range_bound_batch(const BatchMember* M, const long long* node_begin, int nm,
+                                    long long NP, const long long* exc, const long long* cap,
+                                    unsigned long long* out_max) {
+  const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long mx = 0;
+  if (gi < NP) {
+    const int i = batch_member_of(node_begin, nm, gi);
+    const BatchMember& m = M[i];
+    const long long li = gi - m.node_base;
+    const Geo& g = m.g;
+    const int c = int(li % g.Cp), b = int((li / g.Cp) % g.Bp), a = int(li / ((long long)g.Cp * g.Bp));
+    const long long e = exc[gi];
+    unsigned long long s = (unsigned long long)(e < 0 ? -e : e);
+    const long long* cp = cap + m.res_base;
+    for (int k = 0; k < m.st.K; ++k) {
+      s += (unsigned long long)cp[(long long)k * g.NP + li];
+      const int na = a + m.st.da[k], nb = b + m.st.db[k], nc = c + m.st.dc[k];
+      if (na >= 0 && na < g.Ap && nb >= 0 && nb < g.Bp && nc >= 0 && nc < g.Cp) {
+        const long long v = ((long long)na * g.Bp + nb) * g.Cp + nc;
+        s += (unsigned long long)cp[(long long)m.st.rev[k] * g.NP + v];
+      }
+    }
+    mx = s;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_down_sync(0xffffffffu, mx, o);
+    mx = x > mx ? x : mx;
+  }
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(out_max, mx);
+}
+
+// k_extract_cuts for every lattice: thread = one node of the packed output
+__global__ void k_extract_cuts_batch(const BatchMember* M, const long long* out_begin, int nm,
+                                     long long total, const int* mark, const int* h, int* cut_min,
+                                     int* cut_max) {
+  const long long x = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= total) return;
+  const int i = batch_member_of(out_begin, nm, x);
+  const BatchMember& m = M[i];
+  const long long gi = m.node_base + batch_local_node(m, x - out_begin[i]);
+  if (cut_min) cut_min[x] = mark[gi] ? 1 : 0;
+  if (cut_max) cut_max[x] = h[gi] >= kHInf ? 1 : 0;
+}
+
+static inline int bblk(long long n, int t) { return int((n + t - 1) / t); }
+
+// The lattice table of the batch-wide kernels: members, then the first
+// padded node, first packed output node and first packed filling edge of
+// each lattice (three arrays of nm + 1 entries).
+void Batch::upload_table() {
+  if (table_ok) return;
+  const int nm = int(members.size());
+  std::vector<BatchMember> h(nm);
+  std::vector<long long> begins(3 * (size_t)(nm + 1));
+  long long no = 0, eo = 0;
+  for (int i = 0; i < nm; ++i) {
+    const Member& m = members[i];
+    BatchMember& b = h[i];
+    b.g = m.g;
+    b.st = m.st;
+    b.node_base = m.node_base;
+    b.res_base = m.res_base;
+    b.node_off = no;
+    b.edge_off = eo;
+    b.nd = m.nd;
+    begins[i] = m.node_base;
+    begins[(nm + 1) + i] = no;
+    begins[2 * (nm + 1) + i] = eo;
+    no += m.N;
+    eo += m.N * (m.st.K / 2);
+  }
+  begins[nm] = NP;
+  begins[(nm + 1) + nm] = no;
+  begins[2 * (nm + 1) + nm] = eo;
+  if (!d_table) {
+    check(cudaMalloc(&d_table, nm * sizeof(BatchMember)), "cudaMalloc");
+    check(cudaMalloc(&d_begins, begins.size() * sizeof(long long)), "cudaMalloc");
+  }
+  check(cudaMemcpyAsync(d_table, h.data(), nm * sizeof(BatchMember), cudaMemcpyHostToDevice, stream),
+        "memcpy");
+  check(cudaMemcpyAsync(d_begins, begins.data(), begins.size() * sizeof(long long),
+                        cudaMemcpyHostToDevice, stream),
+        "memcpy");
+  // the host vectors go away with this call: the copies finish first
+  check(cudaStreamSynchronize(stream), "sync");
+  table_ok = true;
+}
 
 void Batch::check(cudaError_t e, const char* what) const {
   if (e != cudaSuccess) {
@@ -35,8 +206,14 @@ Batch::~Batch() {
 
 void Batch::release() {
   for (void* p : {(void*)d_exc64, (void*)d_cap64, (void*)d_c0, (void*)d_err, (void*)d_u64,
-                  d_res, d_exc, (void*)d_h, (void*)d_mask, (void*)d_mark})
+                  d_res, d_exc, (void*)d_h, (void*)d_mask, (void*)d_mark, d_table,
+                  (void*)d_begins, d_stage})
     cudaFree(p);
+  d_stage = nullptr;
+  stage_bytes = 0;
+  d_table = nullptr;
+  d_begins = nullptr;
+  table_ok = false;
   d_exc64 = d_cap64 = d_c0 = nullptr;
   d_err = nullptr;
   d_u64 = nullptr;
@@ -92,6 +269,7 @@ void Batch::layout(int elem) {
   NP = nb;
   RES = rb;
   tiles = tb;
+  table_ok = false;
 }
 
 void Batch::alloc_accumulators() {
@@ -150,48 +328,60 @@ void Batch::add_caps_packed(const int32_t* src, const int32_t* snk, const int32_
     nodes += m.N;
     edges += m.N * (m.st.K / 2);
   }
-  // pinned caller arrays are read in place by the fill kernels (the transfer
-  // overlaps the fills); pageable ones are copied to a staging buffer first
-  DevBuf<int32_t> stage;
-  const int32_t* ms = (const int32_t*)mapped_host_ptr(src);
-  const int32_t* mt = (const int32_t*)mapped_host_ptr(snk);
-  const int32_t* me = (const int32_t*)mapped_host_ptr(edge);
-  if ((src && !ms) || (snk && !mt) || (edge && !me)) stage.alloc(size_t(2 * nodes + edges) + 1, stream);
+  // pinned caller arrays are read in place by the fill kernel (host_stage 0;
+  // the transfer overlaps the fill) or moved by the copy engine into a
+  // staging buffer the batch keeps (host_stage 1: whole-array copies instead
+  // of the fill's 4-byte reads over the host link); pageable ones are always
+  // copied into that buffer first
+  const bool stage_pinned = tune.host_stage == 1;
+  const int32_t* ms = stage_pinned ? nullptr : (const int32_t*)mapped_host_ptr(src);
+  const int32_t* mt = stage_pinned ? nullptr : (const int32_t*)mapped_host_ptr(snk);
+  const int32_t* me = stage_pinned ? nullptr : (const int32_t*)mapped_host_ptr(edge);
+  int32_t* stage = nullptr;
+  if ((src && !ms) || (snk && !mt) || (edge && !me)) {
+    const size_t want = size_t(2 * nodes + edges + 1) * sizeof(int32_t);
+    if (stage_bytes < want) {
+      check(cudaStreamSynchronize(stream), "sync");
+      cudaFree(d_stage);
+      d_stage = nullptr;
+      stage_bytes = 0;
+      check(cudaMalloc(&d_stage, want), "cudaMalloc staging");
+      stage_bytes = want;
+    }
+    stage = static_cast<int32_t*>(d_stage);
+  }
   const int32_t* ds = nullptr;
   const int32_t* dt = nullptr;
   const int32_t* de = nullptr;
   if (src) {
     ds = ms;
     if (!ds) {
-      check(cudaMemcpyAsync(stage.p, src, nodes * 4, cudaMemcpyHostToDevice, stream), "memcpy");
-      ds = stage.p;
+      check(cudaMemcpyAsync(stage, src, nodes * 4, cudaMemcpyHostToDevice, stream), "memcpy");
+      ds = stage;
     }
   }
   if (snk) {
     dt = mt;
     if (!dt) {
-      check(cudaMemcpyAsync(stage.p + nodes, snk, nodes * 4, cudaMemcpyHostToDevice, stream), "memcpy");
-      dt = stage.p + nodes;
+      check(cudaMemcpyAsync(stage + nodes, snk, nodes * 4, cudaMemcpyHostToDevice, stream), "memcpy");
+      dt = stage + nodes;
     }
   }
   if (edge) {
     de = me;
     if (!de) {
-      check(cudaMemcpyAsync(stage.p + 2 * nodes, edge, edges * 4, cudaMemcpyHostToDevice, stream),
+      check(cudaMemcpyAsync(stage + 2 * nodes, edge, edges * 4, cudaMemcpyHostToDevice, stream),
             "memcpy");
-      de = stage.p + 2 * nodes;
+      de = stage + 2 * nodes;
     }
   }
-  long long no = 0, eo = 0;
-  for (size_t i = 0; i < members.size(); ++i) {
-    Member& m = members[i];
-    check(launch_fill_caps(m.g, m.st, m.nd, m.N, ds ? ds + no : nullptr, dt ? dt + no : nullptr,
-                           de ? de + eo : nullptr, d_exc64 + m.node_base, d_cap64 + m.res_base,
-                           d_c0 + i, d_err, 0, stream),
-          "fill caps");
-    no += m.N;
-    eo += m.N * (m.st.K / 2);
-  }
+  upload_table();
+  const int nm = int(members.size());
+  if (edges > 0)
+    k_fill_caps_batch<<<bblk(edges, 256), 256, 0, stream>>>(
+        static_cast<const BatchMember*>(d_table), d_begins + 2 * (nm + 1), nm, edges, ds, dt, de,
+        d_exc64, d_cap64, d_c0, d_err);
+  check(cudaGetLastError(), "fill caps");
   solved = false;
   if (!defer_checks) check_err("capacities must be non-negative");
 }
@@ -222,9 +412,12 @@ void Batch::run() {
   stats = SolveStats();
   // 32-bit working arrays when every member fits
   check(cudaMemsetAsync(d_u64, 0, sizeof(unsigned long long), stream), "memset");
-  for (Member& m : members)
-    check(launch_range_bound(m.g, m.st, d_exc64 + m.node_base, d_cap64 + m.res_base, d_u64, stream),
-          "range bound");
+  upload_table();
+  if (NP > 0)
+    k_range_bound_batch<<<bblk(NP, 256), 256, 0, stream>>>(
+        static_cast<const BatchMember*>(d_table), d_begins, int(members.size()), NP, d_exc64,
+        d_cap64, d_u64);
+  check(cudaGetLastError(), "range bound");
   unsigned long long bound = 0;
   check(cudaMemcpyAsync(&h_bound, d_u64, sizeof(h_bound), cudaMemcpyDeviceToHost, stream), "memcpy");
   check(cudaStreamSynchronize(stream), "sync");
@@ -307,16 +500,17 @@ void Batch::fetch_cuts() {
   DevBuf<int> stage;
   stage.alloc(2 * std::max<long long>(total, 1), stream);
   int* buf = stage.p;
-  long long off = 0;
-  for (Member& m : members) {
-    check(launch_extract_cuts(m.g, m.nd, m.N, d_mark + m.node_base, d_h + m.node_base, buf + off,
-                              buf + total + off, stream), "extract cuts");
-    off += m.N;
-  }
+  upload_table();
+  const int nm = int(members.size());
+  if (total > 0)
+    k_extract_cuts_batch<<<bblk(total, 256), 256, 0, stream>>>(
+        static_cast<const BatchMember*>(d_table), d_begins + (nm + 1), nm, total, d_mark, d_h, buf,
+        buf + total);
+  check(cudaGetLastError(), "extract cuts");
   host_cuts.resize(2 * total);
   check(cudaMemcpyAsync(host_cuts.data(), buf, 2 * total * sizeof(int), cudaMemcpyDeviceToHost, stream), "memcpy");
   check(cudaStreamSynchronize(stream), "sync");
-  off = 0;
+  long long off = 0;
   for (Member& m : members) {
     m.cut_off = off;
     off += m.N;
@@ -338,14 +532,13 @@ void Batch::get_cuts_packed(int* out, bool maximal) {
   for (Member& m : members) total += m.N;
   DevBuf<int> stage;
   stage.alloc(std::max<long long>(total, 1), stream);
-  long long off = 0;
-  for (Member& m : members) {
-    check(launch_extract_cuts(m.g, m.nd, m.N, d_mark + m.node_base, d_h + m.node_base,
-                              maximal ? nullptr : stage.p + off, maximal ? stage.p + off : nullptr,
-                              stream),
-          "extract cuts");
-    off += m.N;
-  }
+  upload_table();
+  const int nm = int(members.size());
+  if (total > 0)
+    k_extract_cuts_batch<<<bblk(total, 256), 256, 0, stream>>>(
+        static_cast<const BatchMember*>(d_table), d_begins + (nm + 1), nm, total, d_mark, d_h,
+        maximal ? nullptr : stage.p, maximal ? stage.p : nullptr);
+  check(cudaGetLastError(), "extract cuts");
   check(cudaMemcpyAsync(out, stage.p, total * sizeof(int), cudaMemcpyDeviceToHost, stream), "memcpy");
   check(cudaStreamSynchronize(stream), "sync");
 }

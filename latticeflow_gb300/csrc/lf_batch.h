@@ -54,6 +54,7 @@ class Batch {
   void layout(int elem);
   void alloc_accumulators();
   void fetch_cuts();
+  void upload_table();
 
   bool laid_out = false, runner_ready = false, cuts_fetched = false;
   long long NP = 0, RES = 0, cut_total = 0;
@@ -65,6 +66,11 @@ class Batch {
   int* d_h = nullptr;
   uint64_t* d_mask = nullptr;
   int* d_mark = nullptr;
+  void* d_table = nullptr;       // lattice table of the batch-wide kernels
+  long long* d_begins = nullptr;  // first node / packed node / packed edge per lattice
+  bool table_ok = false;
+  void* d_stage = nullptr;  // kept staging buffer of the packed fill
+  size_t stage_bytes = 0;
   int h_err = 0;
   unsigned long long h_bound = 0;
   std::vector<int> host_cuts;

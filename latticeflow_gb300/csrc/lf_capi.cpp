@@ -619,6 +619,7 @@ int lf_batch_set_param(lf_batch* b, const char* name, int value) {
     else if (n == "bfs_kernel") t.bfs_kernel = value;
     else if (n == "device_loops") t.device_loops = value;
     else if (n == "fill_kernel") t.fill_kernel = value;
+    else if (n == "host_stage") t.host_stage = value;
     else if (n == "defer_checks") b->b->defer_checks = value != 0;
     else throw lfg::LfError{LF_ERR_INVALID, "unknown parameter " + n};
   });

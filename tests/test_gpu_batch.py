@@ -161,3 +161,15 @@ def test_batch_packed_fill_and_results(native, gpu, oracle_port):
     B.run()
     assert np.array_equal(B.getCutsPacked(out=pinned(np.zeros(cuts.size, np.int32))), cuts)
     assert np.array_equal(B.flows()[1], energies)
+    # the same pinned arrays moved into the batch's kept staging buffer by the
+    # copy engine first (twice: the buffer is reused)
+    B.setParam("host_stage", 1)
+    for _ in range(2):
+        B.clear()
+        B.addCapacitiesPacked(pinned(np.concatenate([p.source for p in probs])),
+                              pinned(np.concatenate([p.sink for p in probs])),
+                              pinned(np.concatenate([p.edge.reshape(-1) for p in probs])))
+        B.run()
+        assert np.array_equal(B.getCutsPacked(), cuts)
+        assert np.array_equal(B.getCutsPacked(maximal=True), cuts_max)
+        assert np.array_equal(B.flows()[1], energies)
