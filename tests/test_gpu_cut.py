@@ -304,6 +304,30 @@ def test_tma_pass_3d(native, gpu, oracle_port, pr_kernel, bfs_kernel, kernel, di
         assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
 
 
+def test_tma_bfs_3d_int64(native, gpu, oracle_port):
+    """Capacities beyond 32 bits on a 3-d lattice: 64-bit working arrays, the
+    generic push/relabel pass and the staged 3-d BFS (it reads only masks and
+    heights) give the reference's exact answer."""
+    import latticeflow_gb300 as lf
+    rng = np.random.default_rng(9)
+    kernel, dims = "Full3d_26", (8, 12, 40)
+    offs, _ = oracle_port.lattice_offsets(kernel)
+    N, Kp = int(np.prod(dims)), len(offs) // 2
+    u = rng.integers(0, 3 * 10 ** 9, size=(N, 2)).astype(np.int64)
+    w = rng.integers(0, 10 ** 9, size=(N, Kp)).astype(np.int64)
+    b = np.zeros((N, Kp, 4), np.int64)
+    b[:, :, 1] = w
+    b[:, :, 2] = w
+    E, cmin, cmax, _, _ = oracle_port.port_canonical(kernel, dims, u, b)
+    L = lf.LatticeFlow(kernel, "LatticeEnergyMinimizer", dims)
+    L.setTuning(tile_rows=2, local_sweeps=2, launches_per_relabel=8)
+    L.addEnergyPotentials(u, b)
+    L.run()
+    assert L.layout()[2] == 8
+    assert L.flow()[1] == E
+    assert np.array_equal(L.getCut(), cmin) and np.array_equal(L.getCutMax(), cmax)
+
+
 @pytest.mark.parametrize("tile_rows", [2, 4])
 def test_tma_pass_3d_volume(native, gpu, oracle_port, tile_rows):
     """A 96^3 Full3d_26 volume (the volume workload's generator) through the
