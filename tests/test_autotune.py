@@ -47,3 +47,17 @@ def test_tune_picks_median_fastest_and_caches(tmp_path):
 def test_problem_key_buckets_sizes():
     assert autotune.problem_key(["Full2d_8", "Full2d_4", "Full2d_8"], 4096) == "Full2d_4+Full2d_8|12"
     assert autotune.size_class(1) == 0
+
+
+def test_grids_use_known_knobs():
+    """Every knob of the default grids is one the C ABI's parameter setter
+    accepts (lf_set_param), and every value is a positive integer."""
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                            "latticeflow_gb300", "csrc", "lf_capi.cpp")).read()
+    known = set(re.findall(r'n == "([a-z_]+)"', src))
+    for grid in (autotune.DEFAULT_GRID, autotune.VOLUME_GRID):
+        for name, values in grid.items():
+            assert name in known, name
+            assert values and all(isinstance(v, int) and v >= 0 for v in values), name
