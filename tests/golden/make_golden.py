@@ -60,6 +60,9 @@ PATH_CASES = [
     ("f4_rand_unsorted", "Full2d_4", ("rand", (33, 30), 24), ("list", [0.3, -0.5, 0.01, 2.0, 0.07])),
     ("f4_line", "Full2d_4", ("rand", (1, 40), 25), ("list", [0.1, 1.0])),
     ("f4_poly64", "Full2d_4", ("poly", 64, 8, 26), ("geom", 64)),
+    # regions above the GPU's one-block probe bound (2,048 nodes): probes on
+    # the lattice-wide solver
+    ("f4_poly128", "Full2d_4", ("poly", 128, 12, 27), ("geom", 24)),
 ]
 
 
@@ -108,7 +111,15 @@ def make_energies(kernel, dims, gen, seed):
 def main():
     if not O.ref_available() and not O.build_ref():
         raise SystemExit("compiled reference not available")
+    # optional names of fixtures to (re)make, e.g. "path_f4_poly128"; all by default
+    only = set(sys.argv[1:])
+
+    def wanted(kind, name):
+        return not only or "%s_%s" % (kind, name) in only
+
     for name, kernel, dims, gen, seed in CUT_CASES:
+        if not wanted("cut", name):
+            continue
         u, b = make_energies(kernel, dims, gen, seed)
         pr, _ = O.ref_solve("LatticeEnergyMinimizer", kernel, dims, u, b)
         bk, _ = O.ref_solve("BKGCEnergyMinimizer", kernel, dims, u, b)
@@ -119,12 +130,16 @@ def main():
                             bk_cut=bk.astype(np.int8), energy=np.int64(e))
         print(name, e, int(bk.sum()), int(pr.sum()))
     for name, kernel, dims, lam, seed in TV_CASES:
+        if not wanted("tv", name):
+            continue
         f = np.random.default_rng(seed).random(dims)
         out, _ = O.ref_tv_single(kernel, f, lam)
         np.savez_compressed(os.path.join(OUT, "tv_%s.npz" % name), kernel=kernel, f=f,
                             lam=np.float64(lam), out=out)
         print(name, float(out.min()), float(out.max()), len(np.unique(out)))
     for name, kernel, image, lams in PATH_CASES:
+        if not wanted("path", name):
+            continue
         f, lv = path_inputs(image, lams)
         out, _ = O.ref_tv_path(kernel, f, lv)
         again, _ = O.ref_tv_path(kernel, f, lv)
