@@ -113,7 +113,7 @@ bool bfs3_maps_for(const PoolBFS& p, int TA, int TB, BFS3dMaps& out) {
   const cuuint32_t bm[3] = {32, (cuuint32_t)TB, (cuuint32_t)TA};
   if (!encode_tensor_map(&m.h, p.h, 3, d3, s4, bh) ||
       !encode_tensor_map(&m.mask, const_cast<uint64_t*>(p.mask), 3, d3, s8, bm,
-               CU_TENSOR_MAP_DATA_TYPE_UINT64))
+                         CU_TENSOR_MAP_DATA_TYPE_UINT64))
     return false;
   c.h = p.h; c.mask = p.mask; c.Cp = g.Cp; c.Bp = g.Bp; c.Ap = g.Ap; c.TA = TA; c.TB = TB;
   c.maps = m;
